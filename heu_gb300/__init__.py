@@ -1,0 +1,9 @@
+"""GB300-native Paillier engine with HEU ZPaillier (paillier_z) semantics.
+
+The compute path is the CUDA library built from ``heu_gb300/csrc`` and
+reached through the C-ABI declared in ``include/heu_gb300.h``; there is no
+CPU fallback.
+"""
+
+from heu_gb300.capi import HgError, load  # noqa: F401
+from heu_gb300.engine import Context, Key, ints_to_limbs, keygen, limbs_to_ints  # noqa: F401

@@ -1,0 +1,973 @@
+// Host engine behind the C-ABI (include/heu_gb300.h): contexts, key
+// precompute and residency, device staging, and the multi-kernel sequences
+// (product-tree inverse, reduction levels, fixed-base table build).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <condition_variable>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/heu_gb300.h"
+#include "host_bn.hpp"
+#include "paillier_kernels.cuh"
+
+namespace {
+
+using hg::BN;
+
+thread_local std::string g_last_error;
+
+struct HgError : std::runtime_error {
+  int code;
+  HgError(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+[[noreturn]] void fail(int code, const std::string& msg) { throw HgError(code, msg); }
+
+void cuda_check(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) {
+    if (e == cudaErrorMemoryAllocation) fail(HG_ERR_NOMEM, std::string(what) + ": " + cudaGetErrorString(e));
+    fail(HG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+  }
+}
+
+template <typename F>
+int guarded(F&& f) {
+  try {
+    return f();
+  } catch (const HgError& e) {
+    g_last_error = e.what();
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    g_last_error = "host allocation failed";
+    return HG_ERR_NOMEM;
+  } catch (const std::exception& e) {
+    g_last_error = e.what();
+    return HG_ERR_INVALID;
+  }
+}
+
+// grow-only device buffer
+struct DevBuf {
+  void* p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() {
+    if (p) cudaFree(p);
+  }
+  template <typename T = void>
+  T* ensure(size_t bytes) {
+    if (bytes > n) {
+      if (p) cudaFree(p);
+      p = nullptr;
+      n = 0;
+      cuda_check(cudaMalloc(&p, bytes), "cudaMalloc");
+      n = bytes;
+    }
+    return reinterpret_cast<T*>(p);
+  }
+  template <typename T>
+  T* as() const {
+    return reinterpret_cast<T*>(p);
+  }
+};
+
+struct PinBuf {
+  void* p = nullptr;
+  size_t n = 0;
+  ~PinBuf() {
+    if (p) cudaFreeHost(p);
+  }
+  template <typename T = void>
+  T* ensure(size_t bytes) {
+    if (bytes > n) {
+      if (p) cudaFreeHost(p);
+      p = nullptr;
+      n = 0;
+      cuda_check(cudaMallocHost(&p, bytes), "cudaMallocHost");
+      n = bytes;
+    }
+    return reinterpret_cast<T*>(p);
+  }
+};
+
+uint32_t neg_inv32(uint32_t a) {
+  uint32_t inv = 1;
+  for (int i = 0; i < 5; ++i) inv *= 2u - a * inv;
+  return 0u - inv;
+}
+
+// ---------------------------------------------------------------------------
+// keys
+// ---------------------------------------------------------------------------
+struct KeyRec {
+  int key_bits = 0;
+  int S = 0, Sp = 0, H = 0;
+  bool secret = false;
+  BN n, N, hs, p, q;
+  DevBuf consts, sconsts, table, progs;
+  hg::KeyConst kc{};
+  hg::SecConst sc{};
+  int grid_mul = 0, grid_dec = 0;
+  int wm = 4;  // scalar-mul window
+};
+
+// Sliding-window exponent program: first window index + one op per step.
+void build_prog(const BN& e, int w, int* start, std::vector<uint16_t>* steps) {
+  int i = (int)e.bitlen() - 1;
+  bool first = true;
+  *start = 0;
+  while (i >= 0) {
+    if (!e.bit((size_t)i)) {
+      if (!first) steps->push_back(hg::kOpSquare);
+      --i;
+      continue;
+    }
+    int j = std::max(i - w + 1, 0);
+    while (!e.bit((size_t)j)) ++j;
+    uint32_t val = 0;
+    for (int b = i; b >= j; --b) val = (val << 1) | (e.bit((size_t)b) ? 1u : 0u);
+    const uint16_t idx = (uint16_t)((val - 1) >> 1);
+    if (first) {
+      *start = idx;
+      first = false;
+    } else {
+      for (int s = 0; s < i - j + 1; ++s) steps->push_back(hg::kOpSquare);
+      steps->push_back(idx);
+    }
+    i = j - 1;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// per-call working state: stream, staging, scratch, error word
+// ---------------------------------------------------------------------------
+struct Work {
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  DevBuf io[6];
+  DevBuf scratch, tree, red[2], zbuf;
+  DevBuf err;
+  PinBuf pin_root, pin_err;
+  ~Work() {
+    if (own_stream && stream) cudaStreamDestroy(stream);
+  }
+  uint32_t* errp() { return err.ensure<uint32_t>(sizeof(uint32_t)); }
+};
+
+}  // namespace
+
+struct hg_ctx {
+  int device = 0;
+  int sm_count = 0;
+  std::mutex mu;  // guards keys and the lane pool
+  std::map<int, std::unique_ptr<KeyRec>> keys;
+  int next_key = 1;
+  std::vector<std::unique_ptr<Work>> lanes;
+  std::vector<Work*> free_lanes;
+  std::condition_variable lane_cv;
+  std::mutex dev_mu;  // guards dev_work
+  std::map<cudaStream_t, std::unique_ptr<Work>> dev_work;
+  DevBuf dev_err;
+};
+
+namespace {
+
+constexpr int kLanes = 4;
+
+KeyRec* get_key(hg_ctx* ctx, int id) {
+  if (!ctx) fail(HG_ERR_INVALID, "null context");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  auto it = ctx->keys.find(id);
+  if (it == ctx->keys.end()) fail(HG_ERR_INVALID, "unknown key id " + std::to_string(id));
+  return it->second.get();
+}
+
+struct LaneGuard {
+  hg_ctx* ctx;
+  Work* w;
+  explicit LaneGuard(hg_ctx* c) : ctx(c) {
+    std::unique_lock<std::mutex> lk(ctx->mu);
+    ctx->lane_cv.wait(lk, [&] { return !ctx->free_lanes.empty(); });
+    w = ctx->free_lanes.back();
+    ctx->free_lanes.pop_back();
+  }
+  ~LaneGuard() {
+    {
+      std::lock_guard<std::mutex> lk(ctx->mu);
+      ctx->free_lanes.push_back(w);
+    }
+    ctx->lane_cv.notify_one();
+  }
+};
+
+void set_device(hg_ctx* ctx) { cuda_check(cudaSetDevice(ctx->device), "cudaSetDevice"); }
+
+void reset_err(Work& w) { cuda_check(cudaMemsetAsync(w.errp(), 0, sizeof(uint32_t), w.stream), "memset err"); }
+
+void raise_err_bits(uint32_t bits) {
+  if (bits & hg::kErrCtRange) fail(HG_ERR_CT_RANGE, "Invalid ciphertext: value >= n^2");
+  if (bits & hg::kErrPtRange) fail(HG_ERR_PT_RANGE, "message number out of range: |m| > n/2");
+  if (bits & hg::kErrNotInvertible) fail(HG_ERR_NOT_INVERTIBLE, "ciphertext not invertible mod n^2");
+}
+
+void finish(Work& w) {
+  uint32_t* h = w.pin_err.ensure<uint32_t>(sizeof(uint32_t));
+  cuda_check(cudaMemcpyAsync(h, w.errp(), sizeof(uint32_t), cudaMemcpyDeviceToHost, w.stream), "D2H err");
+  cuda_check(cudaStreamSynchronize(w.stream), "stream sync");
+  raise_err_bits(*h);
+}
+
+void h2d(void* d, const void* h, size_t bytes, Work& w) {
+  if (bytes) cuda_check(cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, w.stream), "H2D");
+}
+void d2h(void* h, const void* d, size_t bytes, Work& w) {
+  if (bytes) cuda_check(cudaMemcpyAsync(h, d, bytes, cudaMemcpyDeviceToHost, w.stream), "D2H");
+}
+
+// ---------------------------------------------------------------------------
+// core device sequences (device pointers, asynchronous except the inverse)
+// ---------------------------------------------------------------------------
+size_t ct_bytes(const KeyRec& k) { return (size_t)k.S * 4; }
+
+void core_encrypt(KeyRec& k, Work& w, hg::EncMode mode, const int64_t* m, const uint32_t* m_mag,
+                  const uint8_t* m_neg, const uint32_t* r, const uint32_t* ct_in, uint32_t* out, size_t count) {
+  cuda_check(hg::launch_encrypt(k.S, k.kc, mode, m, m_mag, m_neg, r, ct_in, out, count, w.errp(), 0, w.stream),
+             "encrypt launch");
+}
+
+void core_decrypt(KeyRec& k, Work& w, const uint32_t* ct, int64_t* m, uint8_t* ovf, uint32_t* mag, uint8_t* neg,
+                  size_t count) {
+  if (!k.secret) fail(HG_ERR_NO_SECRET, "key has no secret part");
+  const size_t ntab = (size_t)1 << (k.sc.wd - 1);
+  const size_t units = (size_t)k.grid_dec * hg::units_per_block_decrypt(k.Sp);
+  uint32_t* scratch = w.scratch.ensure<uint32_t>(units * 2 * ntab * k.Sp * 4);
+  cuda_check(hg::launch_decrypt(k.Sp, k.kc, k.sc, ct, count, m, ovf, mag, neg, scratch, w.errp(), k.grid_dec,
+                                w.stream),
+             "decrypt launch");
+}
+
+// out[i] = in[i]^-1 where sel == nullptr or sel[i] < 0, else in[i].
+void core_inverse(KeyRec& k, Work& w, const uint32_t* in, const int64_t* sel, uint32_t* out, size_t count) {
+  if (count == 0) return;
+  size_t padded = 1;
+  while (padded < count) padded <<= 1;
+  const size_t S = (size_t)k.S;
+  // level l occupies [off_l, off_l + padded >> l)
+  std::vector<size_t> off;
+  size_t total = 0;
+  for (size_t sz = padded;; sz >>= 1) {
+    off.push_back(total);
+    total += sz;
+    if (sz == 1) break;
+  }
+  uint32_t* tr = w.tree.ensure<uint32_t>(total * S * 4);
+  cuda_check(hg::launch_tree_leaves(k.S, k.kc, in, sel, count, tr, padded, w.errp(), w.stream), "tree leaves");
+  for (size_t l = 0; l + 1 < off.size(); ++l) {
+    const size_t up = padded >> (l + 1);
+    cuda_check(hg::launch_tree_up(k.S, k.kc, tr + off[l] * S, tr + off[l + 1] * S, up, w.stream), "tree up");
+  }
+  uint32_t* root = tr + off.back() * S;
+  uint32_t* hroot = w.pin_root.ensure<uint32_t>(S * 4 + 4);
+  d2h(hroot, root, S * 4, w);
+  d2h(hroot + S, w.errp(), 4, w);
+  cuda_check(cudaStreamSynchronize(w.stream), "stream sync");
+  // a ciphertext >= n^2 among the inputs is reported before invertibility
+  raise_err_bits(hroot[S] & (hg::kErrCtRange | hg::kErrPtRange));
+  const BN x = BN::from_limbs(hroot, S);
+  BN z;
+  try {
+    z = BN::invmod(x, k.N);
+  } catch (const std::exception&) {
+    fail(HG_ERR_NOT_INVERTIBLE, "ciphertext not invertible mod n^2 (Negate/Sub/Mul with k<0)");
+  }
+  z.to_limbs(hroot, S);
+  uint32_t* dz = w.zbuf.ensure<uint32_t>(S * 4);
+  h2d(dz, hroot, S * 4, w);
+  cuda_check(hg::launch_root_fix(k.S, k.kc, dz, root, w.stream), "root fix");
+  for (size_t l = off.size() - 1; l-- > 0;) {
+    const size_t up = padded >> (l + 1);
+    cuda_check(hg::launch_tree_down(k.S, k.kc, tr + off[l] * S, tr + off[l + 1] * S, up, w.stream), "tree down");
+  }
+  cuda_check(hg::launch_tree_apply(k.S, k.kc, in, sel, tr, out, count, w.stream), "tree apply");
+  // keep `hroot` valid until the copy above has been consumed
+  cuda_check(cudaStreamSynchronize(w.stream), "stream sync");
+}
+
+void core_mul(KeyRec& k, Work& w, const uint32_t* a, const int64_t* kk, const int64_t* host_k, uint32_t* out,
+              size_t count) {
+  const size_t ntab = (size_t)1 << (k.wm - 1);
+  const size_t inst = (size_t)k.grid_mul * hg::instances_per_block(k.S);
+  uint32_t* scratch = w.scratch.ensure<uint32_t>(inst * ntab * k.S * 4);
+  cuda_check(hg::launch_mul(k.S, k.kc, a, kk, out, count, scratch, k.wm, w.errp(), k.grid_mul, w.stream),
+             "mul launch");
+  bool any_neg = true;
+  if (host_k) {
+    any_neg = false;
+    for (size_t i = 0; i < count && !any_neg; ++i) any_neg = host_k[i] < 0;
+  }
+  if (any_neg) core_inverse(k, w, out, kk, out, count);
+}
+
+void core_sum(KeyRec& k, Work& w, const uint32_t* a, size_t count, uint32_t* out) {
+  if (count == 0) fail(HG_ERR_INVALID, "you cannot sum an empty tensor");
+  const size_t S = (size_t)k.S;
+  const size_t target = (size_t)std::max(1, 152 * 4 * hg::instances_per_block(k.S));
+  const uint32_t* cur = a;
+  size_t n = count;
+  int which = 0;
+  if (n == 1) {
+    cuda_check(cudaMemcpyAsync(out, a, S * 4, cudaMemcpyDeviceToDevice, w.stream), "copy");
+    return;
+  }
+  while (n > 1) {
+    int chunk = (int)std::min<size_t>(64, std::max<size_t>(2, (n + target - 1) / target));
+    const size_t outn = (n + chunk - 1) / chunk;
+    uint32_t* dst = (outn == 1) ? out : w.red[which].ensure<uint32_t>(outn * S * 4);
+    cuda_check(hg::launch_reduce(k.S, k.kc, cur, n, chunk, dst, w.errp(), w.stream), "reduce launch");
+    cur = dst;
+    n = outn;
+    which ^= 1;
+  }
+}
+
+int load_key(hg_ctx* ctx, uint32_t key_bits, const uint32_t* n_l, const uint32_t* hs_l, const uint32_t* p_l,
+                 const uint32_t* q_l, int window) {
+  if (key_bits % 64 != 0) fail(HG_ERR_UNSUPPORTED, "key size must be a multiple of 64 bits");
+  const int S = (int)key_bits / 16;
+  if (!hg::supported_limbs(S)) fail(HG_ERR_UNSUPPORTED, "no compiled variant for " + std::to_string(key_bits) + "-bit keys");
+  auto k = std::make_unique<KeyRec>();
+  k->key_bits = (int)key_bits;
+  k->S = S;
+  k->Sp = S / 2;
+  k->H = S / 4;
+  k->n = BN::from_limbs(n_l, S / 2);
+  if (!k->n.is_odd() || k->n.bitlen() < 16) fail(HG_ERR_INVALID, "n must be odd");
+  k->N = k->n * k->n;
+  k->hs = BN::from_limbs(hs_l, S);
+  if (k->hs >= k->N) fail(HG_ERR_INVALID, "h_s must be < n^2");
+  const BN R = BN(1).shl(32 * (size_t)S);
+  const BN R1 = R % k->N, R2 = (R1 * R1) % k->N, R3 = (R2 * R1) % k->N;
+  const BN nR2 = (k->n * R2) % k->N;
+  const BN hsm = (k->hs * R1) % k->N;
+  const BN nhalf = k->n.shr(1);
+  const size_t key_size = k->n.bitlen();
+  // device constants: N R1 R2 R3 nR2 hsm (S each), n nhalf (S/2 each)
+  std::vector<uint32_t> hc(7 * (size_t)S);
+  auto put = [&](size_t at, const BN& v, size_t limbs) { v.to_limbs(hc.data() + at, limbs); };
+  put(0, k->N, S);
+  put(S, R1, S);
+  put(2 * S, R2, S);
+  put(3 * S, R3, S);
+  put(4 * S, nR2, S);
+  put(5 * S, hsm, S);
+  put(6 * S, k->n, S / 2);
+  put(6 * S + S / 2, nhalf, S / 2);
+  uint32_t* dc = k->consts.ensure<uint32_t>(hc.size() * 4);
+  cuda_check(cudaMemcpy(dc, hc.data(), hc.size() * 4, cudaMemcpyHostToDevice), "upload consts");
+  auto& kc = k->kc;
+  kc.N = dc;
+  kc.R1 = dc + S;
+  kc.R2 = dc + 2 * S;
+  kc.R3 = dc + 3 * S;
+  kc.nR2 = dc + 4 * S;
+  kc.n = dc + 6 * S;
+  kc.nhalf = dc + 6 * S + S / 2;
+  kc.np = neg_inv32(k->N.d[0]);
+  kc.S = S;
+  kc.w = window > 0 ? window : 12;
+  if (kc.w > 20) fail(HG_ERR_INVALID, "table window must be <= 20");
+  kc.rbits = (int)(key_size / 2);
+  kc.rlimbs = (int)key_bits / 64;
+  kc.npos = (kc.rbits + kc.w - 1) / kc.w;
+  // fixed-base table on the device
+  const size_t ent = ((size_t)1 << kc.w) - 1;
+  uint32_t* tab = k->table.ensure<uint32_t>((size_t)kc.npos * ent * S * 4);
+  kc.table = tab;
+  {
+    DevBuf bases;
+    uint32_t* b = bases.ensure<uint32_t>((size_t)kc.npos * S * 4);
+    cuda_check(hg::launch_table_bases(S, kc, dc + 5 * S, b, nullptr), "table bases");
+    cuda_check(hg::launch_table_level(S, kc, tab, b, -1, nullptr), "table level");
+    for (int lv = 0; lv < kc.w; ++lv) cuda_check(hg::launch_table_level(S, kc, tab, b, lv, nullptr), "table level");
+    cuda_check(cudaDeviceSynchronize(), "table build");
+  }
+  k->grid_mul = hg::resident_blocks_mul(S);
+  if (p_l && q_l) {
+    const int Sp = S / 2, H = S / 4;
+    k->p = BN::from_limbs(p_l, H);
+    k->q = BN::from_limbs(q_l, H);
+    if (k->p * k->q != k->n) fail(HG_ERR_INVALID, "pk and sk are not paired: p*q != n");
+    if (!k->p.is_odd() || !k->q.is_odd()) fail(HG_ERR_INVALID, "p and q must be odd");
+    k->secret = true;
+    const BN p2 = k->p * k->p, q2 = k->q * k->q;
+    const BN R1h = BN(1).shl(32 * (size_t)H);
+    auto hfun = [&](const BN& pr, const BN& pr2) {
+      // secret_key.cc:33-42: h = L((n+1)^(pr-1) mod pr^2)^-1 mod pr
+      const BN g = k->n + BN(1);
+      BN hv = hg::HostMont(pr2).pow(g, pr - BN(1));
+      hv = (hv - BN(1)) / pr;
+      return BN::invmod(hv, pr);
+    };
+    const BN hp = hfun(k->p, p2), hq = hfun(k->q, q2);
+    const BN pinvq = BN::invmod(k->p, k->q);
+    // p2 q2 (Sp) | p q hR_p hR_q inv2_p inv2_q pinvqR (H)
+    std::vector<uint32_t> hs2(2 * (size_t)Sp + 7 * (size_t)H);
+    auto put2 = [&](size_t at, const BN& v, size_t limbs) { v.to_limbs(hs2.data() + at, limbs); };
+    put2(0, p2, Sp);
+    put2(Sp, q2, Sp);
+    size_t o = 2 * (size_t)Sp;
+    put2(o, k->p, H);
+    put2(o + H, k->q, H);
+    put2(o + 2 * H, (hp * R1h) % k->p, H);
+    put2(o + 3 * H, (hq * R1h) % k->q, H);
+    put2(o + 4 * H, BN::invmod(k->p, R1h), H);
+    put2(o + 5 * H, BN::invmod(k->q, R1h), H);
+    put2(o + 6 * H, (pinvq * R1h) % k->q, H);
+    uint32_t* ds = k->sconsts.ensure<uint32_t>(hs2.size() * 4);
+    cuda_check(cudaMemcpy(ds, hs2.data(), hs2.size() * 4, cudaMemcpyHostToDevice), "upload secret consts");
+    auto& sc = k->sc;
+    sc.Sp = Sp;
+    sc.P2[0] = ds;
+    sc.P2[1] = ds + Sp;
+    sc.P[0] = ds + o;
+    sc.P[1] = ds + o + H;
+    sc.hR[0] = ds + o + 2 * H;
+    sc.hR[1] = ds + o + 3 * H;
+    sc.inv2[0] = ds + o + 4 * H;
+    sc.inv2[1] = ds + o + 5 * H;
+    sc.pinvqR = ds + o + 6 * H;
+    sc.np2[0] = neg_inv32(p2.d[0]);
+    sc.np2[1] = neg_inv32(q2.d[0]);
+    sc.np1[0] = neg_inv32(k->p.d[0]);
+    sc.np1[1] = neg_inv32(k->q.d[0]);
+    sc.wd = 5;
+    std::vector<uint16_t> pp, pq;
+    build_prog(k->p - BN(1), sc.wd, &sc.start[0], &pp);
+    build_prog(k->q - BN(1), sc.wd, &sc.start[1], &pq);
+    const size_t len = std::max(pp.size(), pq.size());
+    pp.resize(len, hg::kOpNop);
+    pq.resize(len, hg::kOpNop);
+    sc.prog_len = (int)len;
+    uint16_t* dp = k->progs.ensure<uint16_t>(std::max<size_t>(2 * len, 2) * 2);
+    if (len) {
+      cuda_check(cudaMemcpy(dp, pp.data(), len * 2, cudaMemcpyHostToDevice), "upload prog");
+      cuda_check(cudaMemcpy(dp + len, pq.data(), len * 2, cudaMemcpyHostToDevice), "upload prog");
+    }
+    sc.prog[0] = dp;
+    sc.prog[1] = dp + len;
+    k->grid_dec = hg::resident_blocks_decrypt(Sp);
+  }
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  const int id = ctx->next_key++;
+  ctx->keys[id] = std::move(k);
+  return id;
+}
+
+// key generation (key_generator.cc:26-60) from a seeded stream
+std::vector<uint32_t> small_primes() {
+  std::vector<uint32_t> out;
+  std::vector<bool> sieve(2000, true);
+  for (uint32_t i = 2; i < 2000; ++i) {
+    if (!sieve[i]) continue;
+    out.push_back(i);
+    for (uint32_t j = i * i; j < 2000; j += i) sieve[j] = false;
+  }
+  return out;
+}
+
+bool is_probable_prime(const BN& c, const std::vector<uint32_t>& sp) {
+  if (c < BN(2)) return false;
+  for (uint32_t p : sp) {
+    if (c == BN(p)) return true;
+    if ((c % BN(p)).is_zero()) return false;
+  }
+  const BN cm1 = c - BN(1);
+  BN d = cm1;
+  size_t s = 0;
+  while (!d.is_odd()) {
+    d = d.shr(1);
+    ++s;
+  }
+  hg::HostMont mont(c);
+  for (size_t bi = 0; bi < 20; ++bi) {
+    const BN a(sp[bi]);
+    BN x = mont.pow(a, d);
+    if (x == BN(1) || x == cm1) continue;
+    bool comp = true;
+    for (size_t r = 1; r < s; ++r) {
+      x = (x * x) % c;
+      if (x == cm1) {
+        comp = false;
+        break;
+      }
+    }
+    if (comp) return false;
+  }
+  return true;
+}
+
+BN rand_prime_bbs(hg::Xoshiro& prg, size_t bits, const std::vector<uint32_t>& sp) {
+  while (true) {
+    BN c = prg.randbits(bits);
+    if (c.d.size() < (bits + 31) / 32) c.d.resize((bits + 31) / 32, 0);
+    c.d[(bits - 1) / 32] |= 1u << ((bits - 1) % 32);
+    c.d[0] |= 3u;
+    c.trim();
+    if (is_probable_prime(c, sp)) return c;
+  }
+}
+
+}  // namespace
+
+// ===========================================================================
+// C-ABI
+// ===========================================================================
+extern "C" {
+
+const char* hg_last_error(void) { return g_last_error.c_str(); }
+
+int hg_ctx_create(int device, hg_ctx** out) {
+  return guarded([&] {
+    if (!out) fail(HG_ERR_INVALID, "null out pointer");
+    auto ctx = std::make_unique<hg_ctx>();
+    ctx->device = device;
+    cuda_check(cudaSetDevice(device), "cudaSetDevice");
+    cuda_check(cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device), "attr");
+    for (int i = 0; i < kLanes; ++i) {
+      auto w = std::make_unique<Work>();
+      cuda_check(cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking), "stream create");
+      w->own_stream = true;
+      ctx->free_lanes.push_back(w.get());
+      ctx->lanes.push_back(std::move(w));
+    }
+    *out = ctx.release();
+    return HG_OK;
+  });
+}
+
+int hg_ctx_destroy(hg_ctx* ctx) {
+  return guarded([&] {
+    if (!ctx) return HG_OK;
+    cudaSetDevice(ctx->device);
+    cudaDeviceSynchronize();
+    delete ctx;
+    return HG_OK;
+  });
+}
+
+int hg_device_sm_count(hg_ctx* ctx) { return ctx ? ctx->sm_count : 0; }
+
+int hg_keygen(uint32_t key_bits, uint64_t seed, uint32_t* n_out, uint32_t* p_out, uint32_t* q_out,
+              uint32_t* hs_out) {
+  return guarded([&] {
+    if (key_bits % 64 != 0 || key_bits < 128) fail(HG_ERR_INVALID, "Key size must be a multiple of 64");
+    hg::Xoshiro prg(seed);
+    const auto sp = small_primes();
+    const size_t half = key_bits / 2;
+    BN p, q, n;
+    while (true) {
+      p = rand_prime_bbs(prg, half, sp);
+      while (true) {
+        q = rand_prime_bbs(prg, half, sp);
+        const BN c = BN::gcd(p - BN(1), q - BN(1));
+        const BN diff = p > q ? p - q : q - p;
+        if (c == BN(2) && diff.bitlen() >= half - 2) break;
+      }
+      n = p * q;
+      if (n.bitlen() >= key_bits) break;
+    }
+    BN x;
+    while (true) {
+      x = prg.below(n);
+      if (BN::gcd(x, n) == BN(1)) break;
+    }
+    const BN x2 = (x * x) % n;
+    const BN N = n * n;
+    // h = -x^2 mod n as a residue mod n^2; h_s = h^n mod n^2 (CRT in the
+    // reference, secret_key.cc:45-62; the value is the same)
+    const BN h = N - x2;
+    const BN hs = hg::HostMont(N).pow(h, n);
+    if (n_out) n.to_limbs(n_out, key_bits / 32);
+    if (p_out) p.to_limbs(p_out, key_bits / 64);
+    if (q_out) q.to_limbs(q_out, key_bits / 64);
+    if (hs_out) hs.to_limbs(hs_out, key_bits / 16);
+    return HG_OK;
+  });
+}
+
+int hg_key_load(hg_ctx* ctx, uint32_t key_bits, const uint32_t* n, const uint32_t* h_s, const uint32_t* p,
+                const uint32_t* q, int table_window, int* key_id) {
+  return guarded([&] {
+    if (!ctx || !n || !h_s || !key_id) fail(HG_ERR_INVALID, "null argument");
+    if ((p == nullptr) != (q == nullptr)) fail(HG_ERR_INVALID, "give both p and q or neither");
+    set_device(ctx);
+    *key_id = load_key(ctx, key_bits, n, h_s, p, q, table_window);
+    return HG_OK;
+  });
+}
+
+int hg_key_free(hg_ctx* ctx, int key_id) {
+  return guarded([&] {
+    if (!ctx) fail(HG_ERR_INVALID, "null context");
+    set_device(ctx);
+    cuda_check(cudaDeviceSynchronize(), "sync");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    if (!ctx->keys.erase(key_id)) fail(HG_ERR_INVALID, "unknown key id");
+    return HG_OK;
+  });
+}
+
+int hg_key_shape(hg_ctx* ctx, int key_id, int* ct_limbs, int* r_limbs, int* pt_limbs) {
+  return guarded([&] {
+    KeyRec* k = get_key(ctx, key_id);
+    if (ct_limbs) *ct_limbs = k->S;
+    if (r_limbs) *r_limbs = k->kc.rlimbs;
+    if (pt_limbs) *pt_limbs = k->S / 2;
+    return HG_OK;
+  });
+}
+
+// ---- host-pointer API -------------------------------------------------------
+#define HG_HOST_PROLOGUE                       \
+  KeyRec* k = get_key(ctx, key_id);            \
+  if (count == 0) return HG_OK;                \
+  set_device(ctx);                             \
+  LaneGuard lane(ctx);                         \
+  Work& w = *lane.w;                           \
+  reset_err(w);                                \
+  const size_t cb = ct_bytes(*k);              \
+  (void)cb;
+
+int hg_encrypt(hg_ctx* ctx, int key_id, const int64_t* m, const uint32_t* r, uint32_t* ct_out, size_t count) {
+  return guarded([&] {
+    if (!m || !r || !ct_out) fail(HG_ERR_INVALID, "null argument");
+    HG_HOST_PROLOGUE
+    const size_t rb = (size_t)k->kc.rlimbs * 4;
+    auto* dm = w.io[0].ensure<int64_t>(count * 8);
+    auto* dr = w.io[1].ensure<uint32_t>(count * rb);
+    auto* dout = w.io[2].ensure<uint32_t>(count * cb);
+    h2d(dm, m, count * 8, w);
+    h2d(dr, r, count * rb, w);
+    core_encrypt(*k, w, hg::EncMode::kEncrypt, dm, nullptr, nullptr, dr, nullptr, dout, count);
+    d2h(ct_out, dout, count * cb, w);
+    finish(w);
+    return HG_OK;
+  });
+}
+
+int hg_encrypt_bn(hg_ctx* ctx, int key_id, const uint32_t* m_mag, const uint8_t* m_neg, const uint32_t* r,
+                  uint32_t* ct_out, size_t count) {
+  return guarded([&] {
+    if (!m_mag || !m_neg || !r || !ct_out) fail(HG_ERR_INVALID, "null argument");
+    HG_HOST_PROLOGUE
+    const size_t rb = (size_t)k->kc.rlimbs * 4, pb = (size_t)k->S / 2 * 4;
+    auto* dmag = w.io[0].ensure<uint32_t>(count * pb);
+    auto* dneg = w.io[3].ensure<uint8_t>(count);
+    auto* dr = w.io[1].ensure<uint32_t>(count * rb);
+    auto* dout = w.io[2].ensure<uint32_t>(count * cb);
+    h2d(dmag, m_mag, count * pb, w);
+    h2d(dneg, m_neg, count, w);
+    h2d(dr, r, count * rb, w);
+    core_encrypt(*k, w, hg::EncMode::kEncrypt, nullptr, dmag, dneg, dr, nullptr, dout, count);
+    d2h(ct_out, dout, count * cb, w);
+    finish(w);
+    return HG_OK;
+  });
+}
+
+int hg_encrypt_zero(hg_ctx* ctx, int key_id, const uint32_t* r, uint32_t* ct_out, size_t count) {
+  return guarded([&] {
+    if (!r || !ct_out) fail(HG_ERR_INVALID, "null argument");
+    HG_HOST_PROLOGUE
+    const size_t rb = (size_t)k->kc.rlimbs * 4;
+    auto* dr = w.io[1].ensure<uint32_t>(count * rb);
+    auto* dout = w.io[2].ensure<uint32_t>(count * cb);
+    h2d(dr, r, count * rb, w);
+    core_encrypt(*k, w, hg::EncMode::kZero, nullptr, nullptr, nullptr, dr, nullptr, dout, count);
+    d2h(ct_out, dout, count * cb, w);
+    finish(w);
+    return HG_OK;
+  });
+}
+
+int hg_randomize(hg_ctx* ctx, int key_id, uint32_t* ct, const uint32_t* r, size_t count) {
+  return guarded([&] {
+    if (!r || !ct) fail(HG_ERR_INVALID, "null argument");
+    HG_HOST_PROLOGUE
+    const size_t rb = (size_t)k->kc.rlimbs * 4;
+    auto* dr = w.io[1].ensure<uint32_t>(count * rb);
+    auto* dc = w.io[2].ensure<uint32_t>(count * cb);
+    h2d(dr, r, count * rb, w);
+    h2d(dc, ct, count * cb, w);
+    core_encrypt(*k, w, hg::EncMode::kRandomize, nullptr, nullptr, nullptr, dr, dc, dc, count);
+    d2h(ct, dc, count * cb, w);
+    finish(w);
+    return HG_OK;
+  });
+}
+
+int hg_decrypt(hg_ctx* ctx, int key_id, const uint32_t* ct, int64_t* m_out, uint8_t* overflow, size_t count) {
+  return guarded([&] {
+    if (!ct || !m_out) fail(HG_ERR_INVALID, "null argument");
+    HG_HOST_PROLOGUE
+    auto* dc = w.io[0].ensure<uint32_t>(count * cb);
+    auto* dm = w.io[1].ensure<int64_t>(count * 8);
+    auto* dov = w.io[2].ensure<uint8_t>(count);
+    h2d(dc, ct, count * cb, w);
+    core_decrypt(*k, w, dc, dm, dov, nullptr, nullptr, count);
+    d2h(m_out, dm, count * 8, w);
+    if (overflow) d2h(overflow, dov, count, w);
+    finish(w);
+    return HG_OK;
+  });
+}
+
+int hg_decrypt_bn(hg_ctx* ctx, int key_id, const uint32_t* ct, uint32_t* m_mag, uint8_t* m_neg, size_t count) {
+  return guarded([&] {
+    if (!ct || !m_mag || !m_neg) fail(HG_ERR_INVALID, "null argument");
+    HG_HOST_PROLOGUE
+    const size_t pb = (size_t)k->S / 2 * 4;
+    auto* dc = w.io[0].ensure<uint32_t>(count * cb);
+    auto* dmag = w.io[1].ensure<uint32_t>(count * pb);
+    auto* dneg = w.io[2].ensure<uint8_t>(count);
+    h2d(dc, ct, count * cb, w);
+    core_decrypt(*k, w, dc, nullptr, nullptr, dmag, dneg, count);
+    d2h(m_mag, dmag, count * pb, w);
+    d2h(m_neg, dneg, count, w);
+    finish(w);
+    return HG_OK;
+  });
+}
+
+int hg_add(hg_ctx* ctx, int key_id, const uint32_t* a, const uint32_t* b, uint32_t* out, size_t count) {
+  return guarded([&] {
+    if (!a || !b || !out) fail(HG_ERR_INVALID, "null argument");
+    HG_HOST_PROLOGUE
+    auto* da = w.io[0].ensure<uint32_t>(count * cb);
+    auto* db = w.io[1].ensure<uint32_t>(count * cb);
+    h2d(da, a, count * cb, w);
+    h2d(db, b, count * cb, w);
+    cuda_check(hg::launch_add(k->S, k->kc, da, db, da, count, w.errp(), w.stream), "add launch");
+    d2h(out, da, count * cb, w);
+    finish(w);
+    return HG_OK;
+  });
+}
+
+static int add_plain_impl(hg_ctx* ctx, int key_id, const uint32_t* a, const int64_t* p, int neg, uint32_t* out,
+                          size_t count) {
+  return guarded([&] {
+    if (!a || !p || !out) fail(HG_ERR_INVALID, "null argument");
+    HG_HOST_PROLOGUE
+    auto* da = w.io[0].ensure<uint32_t>(count * cb);
+    auto* dp = w.io[1].ensure<int64_t>(count * 8);
+    h2d(da, a, count * cb, w);
+    h2d(dp, p, count * 8, w);
+    cuda_check(hg::launch_add_plain(k->S, k->kc, da, dp, neg, da, count, w.errp(), w.stream), "add_plain launch");
+    d2h(out, da, count * cb, w);
+    finish(w);
+    return HG_OK;
+  });
+}
+
+int hg_add_plain(hg_ctx* ctx, int key_id, const uint32_t* a, const int64_t* p, uint32_t* out, size_t count) {
+  return add_plain_impl(ctx, key_id, a, p, 0, out, count);
+}
+
+int hg_sub_plain(hg_ctx* ctx, int key_id, const uint32_t* a, const int64_t* p, uint32_t* out, size_t count) {
+  return add_plain_impl(ctx, key_id, a, p, 1, out, count);
+}
+
+int hg_negate(hg_ctx* ctx, int key_id, const uint32_t* a, uint32_t* out, size_t count) {
+  return guarded([&] {
+    if (!a || !out) fail(HG_ERR_INVALID, "null argument");
+    HG_HOST_PROLOGUE
+    auto* da = w.io[0].ensure<uint32_t>(count * cb);
+    h2d(da, a, count * cb, w);
+    core_inverse(*k, w, da, nullptr, da, count);
+    d2h(out, da, count * cb, w);
+    finish(w);
+    return HG_OK;
+  });
+}
+
+int hg_sub(hg_ctx* ctx, int key_id, const uint32_t* a, const uint32_t* b, uint32_t* out, size_t count) {
+  return guarded([&] {
+    if (!a || !b || !out) fail(HG_ERR_INVALID, "null argument");
+    HG_HOST_PROLOGUE
+    auto* da = w.io[0].ensure<uint32_t>(count * cb);
+    auto* db = w.io[1].ensure<uint32_t>(count * cb);
+    h2d(da, a, count * cb, w);
+    h2d(db, b, count * cb, w);
+    // evaluator.cc:66-68: Add(a, Negate(b))
+    core_inverse(*k, w, db, nullptr, db, count);
+    cuda_check(hg::launch_add(k->S, k->kc, da, db, da, count, w.errp(), w.stream), "add launch");
+    d2h(out, da, count * cb, w);
+    finish(w);
+    return HG_OK;
+  });
+}
+
+int hg_plain_sub(hg_ctx* ctx, int key_id, const int64_t* p, const uint32_t* a, uint32_t* out, size_t count) {
+  return guarded([&] {
+    if (!a || !p || !out) fail(HG_ERR_INVALID, "null argument");
+    HG_HOST_PROLOGUE
+    auto* da = w.io[0].ensure<uint32_t>(count * cb);
+    auto* dp = w.io[1].ensure<int64_t>(count * 8);
+    h2d(da, a, count * cb, w);
+    h2d(dp, p, count * 8, w);
+    // evaluator.cc:82-84: Add(Negate(a), p)
+    core_inverse(*k, w, da, nullptr, da, count);
+    cuda_check(hg::launch_add_plain(k->S, k->kc, da, dp, 0, da, count, w.errp(), w.stream), "add_plain launch");
+    d2h(out, da, count * cb, w);
+    finish(w);
+    return HG_OK;
+  });
+}
+
+int hg_mul(hg_ctx* ctx, int key_id, const uint32_t* a, const int64_t* kk, uint32_t* out, size_t count) {
+  return guarded([&] {
+    if (!a || !kk || !out) fail(HG_ERR_INVALID, "null argument");
+    HG_HOST_PROLOGUE
+    auto* da = w.io[0].ensure<uint32_t>(count * cb);
+    auto* dk = w.io[1].ensure<int64_t>(count * 8);
+    auto* dout = w.io[2].ensure<uint32_t>(count * cb);
+    h2d(da, a, count * cb, w);
+    h2d(dk, kk, count * 8, w);
+    core_mul(*k, w, da, dk, kk, dout, count);
+    d2h(out, dout, count * cb, w);
+    finish(w);
+    return HG_OK;
+  });
+}
+
+int hg_sum(hg_ctx* ctx, int key_id, const uint32_t* a, size_t count, uint32_t* out) {
+  return guarded([&] {
+    if (!a || !out) fail(HG_ERR_INVALID, "null argument");
+    if (count == 0) fail(HG_ERR_INVALID, "you cannot sum an empty tensor");
+    HG_HOST_PROLOGUE
+    auto* da = w.io[0].ensure<uint32_t>(count * cb);
+    auto* dout = w.io[1].ensure<uint32_t>(cb);
+    h2d(da, a, count * cb, w);
+    core_sum(*k, w, da, count, dout);
+    d2h(out, dout, cb, w);
+    finish(w);
+    return HG_OK;
+  });
+}
+
+static int convert_impl(hg_ctx* ctx, int key_id, const uint32_t* in, uint32_t* out, size_t count, int to_mont) {
+  return guarded([&] {
+    if (!in || !out) fail(HG_ERR_INVALID, "null argument");
+    HG_HOST_PROLOGUE
+    auto* da = w.io[0].ensure<uint32_t>(count * cb);
+    h2d(da, in, count * cb, w);
+    cuda_check(hg::launch_convert(k->S, k->kc, da, da, count, to_mont, w.errp(), w.stream), "convert launch");
+    d2h(out, da, count * cb, w);
+    finish(w);
+    return HG_OK;
+  });
+}
+
+int hg_to_mont(hg_ctx* ctx, int key_id, const uint32_t* z, uint32_t* mont, size_t count) {
+  return convert_impl(ctx, key_id, z, mont, count, 1);
+}
+
+int hg_from_mont(hg_ctx* ctx, int key_id, const uint32_t* mont, uint32_t* z, size_t count) {
+  return convert_impl(ctx, key_id, mont, z, count, 0);
+}
+
+// ---- device-pointer API -----------------------------------------------------
+static Work& dev_work(hg_ctx* ctx, void* stream) {
+  std::lock_guard<std::mutex> lk(ctx->dev_mu);
+  cudaStream_t st = stream ? (cudaStream_t)stream : ctx->lanes[0]->stream;
+  auto& slot = ctx->dev_work[st];
+  if (!slot) {
+    slot = std::make_unique<Work>();
+    slot->stream = st;
+    slot->own_stream = false;
+    cuda_check(cudaMemsetAsync(slot->errp(), 0, sizeof(uint32_t), st), "memset err");
+  }
+  return *slot;
+}
+
+#define HG_DEV_PROLOGUE                   \
+  KeyRec* k = get_key(ctx, key_id);       \
+  if (count == 0) return HG_OK;           \
+  set_device(ctx);                        \
+  Work& w = dev_work(ctx, stream);
+
+int hg_dev_encrypt(hg_ctx* ctx, int key_id, const int64_t* m, const uint32_t* r, uint32_t* ct_out, size_t count,
+                   void* stream) {
+  return guarded([&] {
+    HG_DEV_PROLOGUE
+    core_encrypt(*k, w, hg::EncMode::kEncrypt, m, nullptr, nullptr, r, nullptr, ct_out, count);
+    return HG_OK;
+  });
+}
+
+int hg_dev_decrypt(hg_ctx* ctx, int key_id, const uint32_t* ct, int64_t* m_out, uint8_t* overflow, size_t count,
+                   void* stream) {
+  return guarded([&] {
+    HG_DEV_PROLOGUE
+    core_decrypt(*k, w, ct, m_out, overflow, nullptr, nullptr, count);
+    return HG_OK;
+  });
+}
+
+int hg_dev_add(hg_ctx* ctx, int key_id, const uint32_t* a, const uint32_t* b, uint32_t* out, size_t count,
+               void* stream) {
+  return guarded([&] {
+    HG_DEV_PROLOGUE
+    cuda_check(hg::launch_add(k->S, k->kc, a, b, out, count, w.errp(), w.stream), "add launch");
+    return HG_OK;
+  });
+}
+
+int hg_dev_mul(hg_ctx* ctx, int key_id, const uint32_t* a, const int64_t* kk, uint32_t* out, size_t count,
+               void* stream) {
+  return guarded([&] {
+    HG_DEV_PROLOGUE
+    core_mul(*k, w, a, kk, nullptr, out, count);
+    return HG_OK;
+  });
+}
+
+int hg_dev_sum(hg_ctx* ctx, int key_id, const uint32_t* a, size_t count, uint32_t* out, void* stream) {
+  return guarded([&] {
+    if (count == 0) fail(HG_ERR_INVALID, "you cannot sum an empty tensor");
+    HG_DEV_PROLOGUE
+    core_sum(*k, w, a, count, out);
+    return HG_OK;
+  });
+}
+
+int hg_dev_check(hg_ctx* ctx) {
+  return guarded([&] {
+    if (!ctx) fail(HG_ERR_INVALID, "null context");
+    set_device(ctx);
+    uint32_t bits = 0;
+    std::lock_guard<std::mutex> lk(ctx->dev_mu);
+    for (auto& kv : ctx->dev_work) {
+      Work& w = *kv.second;
+      uint32_t* h = w.pin_err.ensure<uint32_t>(sizeof(uint32_t));
+      cuda_check(cudaMemcpyAsync(h, w.errp(), sizeof(uint32_t), cudaMemcpyDeviceToHost, w.stream), "D2H err");
+      cuda_check(cudaStreamSynchronize(w.stream), "stream sync");
+      bits |= *h;
+      cuda_check(cudaMemsetAsync(w.errp(), 0, sizeof(uint32_t), w.stream), "memset err");
+    }
+    raise_err_bits(bits);
+    return HG_OK;
+  });
+}
+
+}  // extern "C"

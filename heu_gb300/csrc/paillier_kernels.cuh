@@ -1,0 +1,101 @@
+// Kernel parameter blocks and launcher declarations shared by the kernels
+// (paillier_kernels.cu) and the host engine (engine.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <cstddef>
+#include <cstdint>
+
+namespace hg {
+
+// Error bits raised by kernels into a device word (atomicOr).
+enum : uint32_t {
+  kErrCtRange = 1u,      // a ciphertext >= n^2 reached a kernel
+  kErrNotInvertible = 2u,
+  kErrPtRange = 4u,      // a plaintext with |m| > n/2
+};
+
+// Public-key constants for arithmetic mod N = n^2 with R = 2^(32*S).
+struct KeyConst {
+  const uint32_t* N;    // n^2                         (S limbs)
+  const uint32_t* R1;   // R mod N  (Montgomery one)  (S limbs)
+  const uint32_t* R2;   // R^2 mod N                  (S limbs)
+  const uint32_t* R3;   // R^3 mod N                  (S limbs)
+  const uint32_t* nR2;  // n * R^2 mod N              (S limbs)
+  const uint32_t* n;    // n                          (S/2 limbs)
+  const uint32_t* nhalf;  // floor(n/2)              (S/2 limbs)
+  const uint32_t* table;  // fixed-base table of h_s powers, Montgomery form
+  uint32_t np;          // -N^-1 mod 2^32
+  int S;                // 32-bit limbs of N
+  int w;                // table window (bits per digit)
+  int npos;             // digit positions = ceil(rbits / w)
+  int rbits;            // bits of the encryption randomness r (k/2)
+  int rlimbs;           // 32-bit limbs per r
+};
+
+// Secret-key constants for CRT decryption.  Index 0 = p side, 1 = q side.
+struct SecConst {
+  const uint32_t* P2[2];    // p^2, q^2                    (Sp limbs)
+  const uint32_t* P[2];     // p, q                        (Sp/2 limbs)
+  const uint32_t* hR[2];    // hp*R1 mod p, hq*R1 mod q    (Sp/2 limbs), R1 = 2^(16*Sp)
+  const uint32_t* inv2[2];  // p^-1, q^-1 mod 2^(16*Sp)    (Sp/2 limbs)
+  const uint32_t* pinvqR;   // (p^-1 mod q)*R1 mod q       (Sp/2 limbs)
+  const uint16_t* prog[2];  // exponent programs for p-1, q-1
+  uint32_t np2[2];          // -(p^2)^-1, -(q^2)^-1 mod 2^32
+  uint32_t np1[2];          // -p^-1, -q^-1 mod 2^32
+  int start[2];             // first window's table index
+  int prog_len;             // both programs padded to this many steps
+  int wd;                   // decryption window bits
+  int Sp;                   // 32-bit limbs of p^2
+};
+
+// Exponent-program opcodes (one Montgomery multiplication per step).
+constexpr uint16_t kOpSquare = 0xFFFFu;
+constexpr uint16_t kOpNop = 0xFFFEu;
+
+enum class EncMode : int { kEncrypt = 0, kZero = 1, kRandomize = 2 };
+
+// Launchers.  All are asynchronous on `stream` and return cudaError_t of the
+// launch.  `cfg` selects the (threads per instance, limbs per thread) variant.
+cudaError_t launch_encrypt(int S, const KeyConst& kc, EncMode mode, const int64_t* m, const uint32_t* m_mag,
+                           const uint8_t* m_neg, const uint32_t* r, const uint32_t* ct_in, uint32_t* out,
+                           size_t count, uint32_t* err, int grid, cudaStream_t st);
+cudaError_t launch_add(int S, const KeyConst& kc, const uint32_t* a, const uint32_t* b, uint32_t* out,
+                       size_t count, uint32_t* err, cudaStream_t st);
+cudaError_t launch_add_plain(int S, const KeyConst& kc, const uint32_t* a, const int64_t* p, int neg_p,
+                             uint32_t* out, size_t count, uint32_t* err, cudaStream_t st);
+cudaError_t launch_mul(int S, const KeyConst& kc, const uint32_t* a, const int64_t* k, uint32_t* out,
+                       size_t count, uint32_t* scratch, int wm, uint32_t* err, int grid, cudaStream_t st);
+cudaError_t launch_decrypt(int Sp, const KeyConst& kc, const SecConst& sc, const uint32_t* ct, size_t count,
+                           int64_t* out_i64, uint8_t* out_ovf, uint32_t* out_mag, uint8_t* out_neg,
+                           uint32_t* scratch, uint32_t* err, int grid, cudaStream_t st);
+cudaError_t launch_convert(int S, const KeyConst& kc, const uint32_t* in, uint32_t* out, size_t count,
+                           int to_mont, uint32_t* err, cudaStream_t st);
+cudaError_t launch_reduce(int S, const KeyConst& kc, const uint32_t* in, size_t count, int chunk,
+                          uint32_t* out, uint32_t* err, cudaStream_t st);
+// product tree for batch inversion
+cudaError_t launch_tree_leaves(int S, const KeyConst& kc, const uint32_t* in, const int64_t* sel, size_t count,
+                               uint32_t* leaves, size_t padded, uint32_t* err, cudaStream_t st);
+cudaError_t launch_tree_up(int S, const KeyConst& kc, const uint32_t* lower, uint32_t* upper, size_t upper_count,
+                           cudaStream_t st);
+cudaError_t launch_tree_down(int S, const KeyConst& kc, uint32_t* lower, const uint32_t* upper_inv,
+                             size_t upper_count, cudaStream_t st);
+cudaError_t launch_tree_apply(int S, const KeyConst& kc, const uint32_t* in, const int64_t* sel,
+                              const uint32_t* leaves_inv, uint32_t* out, size_t count, cudaStream_t st);
+cudaError_t launch_root_fix(int S, const KeyConst& kc, const uint32_t* root_inv_z, uint32_t* root_slot,
+                            cudaStream_t st);
+// fixed-base table construction
+cudaError_t launch_table_bases(int S, const KeyConst& kc, const uint32_t* hs_mont, uint32_t* bases,
+                               cudaStream_t st);
+cudaError_t launch_table_level(int S, const KeyConst& kc, uint32_t* table, const uint32_t* bases, int level,
+                               cudaStream_t st);
+
+// Occupancy-derived grid sizes (blocks) for the persistent kernels.
+int resident_blocks_encrypt(int S);
+int resident_blocks_mul(int S);
+int resident_blocks_decrypt(int Sp);
+int instances_per_block(int S);
+int units_per_block_decrypt(int Sp);
+
+bool supported_limbs(int S);
+
+}  // namespace hg

@@ -1,0 +1,228 @@
+"""Python host layer over the C-ABI: contexts, keys and batched operations on
+NumPy arrays.
+
+Names follow HEU's phe / heu.numpy interfaces for the ZPaillier path
+(heu/library/phe/encryptor.h, decryptor.h, evaluator.h; heu/library/numpy/
+evaluator.h): a loaded key exposes encrypt / decrypt / add / sub / mul /
+negate / randomize / sum over batches.  Ciphertexts are uint32 arrays of
+shape (count, S) in Montgomery form (HEU's in-memory representation);
+``from_mont`` gives the canonical Z-form.
+"""
+
+import ctypes
+
+import numpy as np
+
+from heu_gb300 import capi
+
+
+def ints_to_limbs(values, nlimbs):
+    """Non-negative Python ints -> uint32 array (count, nlimbs), little-endian."""
+    nb = 4 * nlimbs
+    buf = b"".join(int(v).to_bytes(nb, "little") for v in values)
+    return np.frombuffer(buf, dtype="<u4").reshape(len(values), nlimbs).copy()
+
+
+def limbs_to_ints(arr):
+    arr = np.ascontiguousarray(arr, dtype="<u4")
+    if arr.ndim == 1:
+        arr = arr.reshape(1, -1)
+    raw = arr.tobytes()
+    nb = arr.shape[1] * 4
+    return [int.from_bytes(raw[i * nb:(i + 1) * nb], "little") for i in range(arr.shape[0])]
+
+
+def _ptr(a):
+    return ctypes.c_void_p(a.ctypes.data) if a is not None else None
+
+
+def _u32(a, shape=None):
+    a = np.ascontiguousarray(a, dtype=np.uint32)
+    if shape is not None and a.shape != shape:
+        a = a.reshape(shape)
+    return a
+
+
+def _i64(a):
+    return np.ascontiguousarray(a, dtype=np.int64).reshape(-1)
+
+
+def keygen(key_bits, seed):
+    """key_generator.cc:26-60 from a seeded stream -> dict of ints n, p, q, h_s."""
+    lib = capi.load()
+    n = np.zeros(key_bits // 32, np.uint32)
+    p = np.zeros(key_bits // 64, np.uint32)
+    q = np.zeros(key_bits // 64, np.uint32)
+    hs = np.zeros(key_bits // 16, np.uint32)
+    capi.check(lib.hg_keygen(key_bits, seed & (2 ** 64 - 1), _ptr(n), _ptr(p), _ptr(q), _ptr(hs)))
+    return {
+        "n": limbs_to_ints(n)[0],
+        "p": limbs_to_ints(p)[0],
+        "q": limbs_to_ints(q)[0],
+        "h_s": limbs_to_ints(hs)[0],
+    }
+
+
+class Context:
+    """One engine context on one device (hg_ctx)."""
+
+    def __init__(self, device=0):
+        self.lib = capi.load()
+        h = ctypes.c_void_p()
+        capi.check(self.lib.hg_ctx_create(device, ctypes.byref(h)))
+        self.handle = h
+        self.device = device
+
+    def close(self):
+        if self.handle:
+            self.lib.hg_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def sm_count(self):
+        return self.lib.hg_device_sm_count(self.handle)
+
+    def load_key(self, key_bits, n, h_s, p=None, q=None, table_window=0):
+        S = key_bits // 16
+        n_l = ints_to_limbs([n], S // 2)
+        hs_l = ints_to_limbs([h_s], S)
+        p_l = ints_to_limbs([p], S // 4) if p is not None else None
+        q_l = ints_to_limbs([q], S // 4) if q is not None else None
+        kid = ctypes.c_int()
+        capi.check(self.lib.hg_key_load(self.handle, key_bits, _ptr(n_l), _ptr(hs_l), _ptr(p_l), _ptr(q_l),
+                                        table_window, ctypes.byref(kid)))
+        return Key(self, kid.value, key_bits, n)
+
+
+class Key:
+    def __init__(self, ctx, key_id, key_bits, n):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        self.id = key_id
+        self.key_bits = key_bits
+        self.n = n
+        s, r, pl = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        capi.check(self.lib.hg_key_shape(ctx.handle, key_id, ctypes.byref(s), ctypes.byref(r), ctypes.byref(pl)))
+        self.ct_limbs, self.r_limbs, self.pt_limbs = s.value, r.value, pl.value
+
+    # -- helpers ----------------------------------------------------------
+    def _ct(self, a):
+        a = np.ascontiguousarray(a, dtype=np.uint32)
+        return a.reshape(-1, self.ct_limbs)
+
+    def _out(self, count):
+        return np.empty((count, self.ct_limbs), dtype=np.uint32)
+
+    def free(self):
+        capi.check(self.lib.hg_key_free(self.ctx.handle, self.id))
+
+    # -- encryption -------------------------------------------------------
+    def encrypt(self, m, r):
+        m = _i64(m)
+        r = _u32(r).reshape(-1, self.r_limbs)
+        out = self._out(m.size)
+        capi.check(self.lib.hg_encrypt(self.ctx.handle, self.id, _ptr(m), _ptr(r), _ptr(out), m.size))
+        return out
+
+    def encrypt_bn(self, ms, r):
+        mags = ints_to_limbs([abs(int(v)) for v in ms], self.pt_limbs)
+        neg = np.array([1 if int(v) < 0 else 0 for v in ms], dtype=np.uint8)
+        r = _u32(r).reshape(-1, self.r_limbs)
+        out = self._out(len(ms))
+        capi.check(self.lib.hg_encrypt_bn(self.ctx.handle, self.id, _ptr(mags), _ptr(neg), _ptr(r), _ptr(out),
+                                          len(ms)))
+        return out
+
+    def encrypt_zero(self, r):
+        r = _u32(r).reshape(-1, self.r_limbs)
+        out = self._out(r.shape[0])
+        capi.check(self.lib.hg_encrypt_zero(self.ctx.handle, self.id, _ptr(r), _ptr(out), r.shape[0]))
+        return out
+
+    def randomize(self, ct, r):
+        out = self._ct(ct).copy()
+        r = _u32(r).reshape(-1, self.r_limbs)
+        capi.check(self.lib.hg_randomize(self.ctx.handle, self.id, _ptr(out), _ptr(r), out.shape[0]))
+        return out
+
+    # -- decryption -------------------------------------------------------
+    def decrypt(self, ct):
+        ct = self._ct(ct)
+        m = np.empty(ct.shape[0], dtype=np.int64)
+        ovf = np.empty(ct.shape[0], dtype=np.uint8)
+        capi.check(self.lib.hg_decrypt(self.ctx.handle, self.id, _ptr(ct), _ptr(m), _ptr(ovf), ct.shape[0]))
+        return m, ovf
+
+    def decrypt_bn(self, ct):
+        ct = self._ct(ct)
+        mag = np.empty((ct.shape[0], self.pt_limbs), dtype=np.uint32)
+        neg = np.empty(ct.shape[0], dtype=np.uint8)
+        capi.check(self.lib.hg_decrypt_bn(self.ctx.handle, self.id, _ptr(ct), _ptr(mag), _ptr(neg), ct.shape[0]))
+        return [(-v if s else v) for v, s in zip(limbs_to_ints(mag), neg)]
+
+    # -- evaluator --------------------------------------------------------
+    def _binary_ct(self, fn, a, b):
+        a, b = self._ct(a), self._ct(b)
+        if a.shape != b.shape:
+            raise ValueError("shape mismatch")
+        out = self._out(a.shape[0])
+        capi.check(fn(self.ctx.handle, self.id, _ptr(a), _ptr(b), _ptr(out), a.shape[0]))
+        return out
+
+    def _ct_pt(self, fn, a, p):
+        a, p = self._ct(a), _i64(p)
+        if a.shape[0] != p.size:
+            raise ValueError("shape mismatch")
+        out = self._out(a.shape[0])
+        capi.check(fn(self.ctx.handle, self.id, _ptr(a), _ptr(p), _ptr(out), a.shape[0]))
+        return out
+
+    def add(self, a, b):
+        return self._binary_ct(self.lib.hg_add, a, b)
+
+    def sub(self, a, b):
+        return self._binary_ct(self.lib.hg_sub, a, b)
+
+    def add_plain(self, a, p):
+        return self._ct_pt(self.lib.hg_add_plain, a, p)
+
+    def sub_plain(self, a, p):
+        return self._ct_pt(self.lib.hg_sub_plain, a, p)
+
+    def plain_sub(self, p, a):
+        a, p = self._ct(a), _i64(p)
+        out = self._out(a.shape[0])
+        capi.check(self.lib.hg_plain_sub(self.ctx.handle, self.id, _ptr(p), _ptr(a), _ptr(out), a.shape[0]))
+        return out
+
+    def mul(self, a, k):
+        return self._ct_pt(self.lib.hg_mul, a, k)
+
+    def negate(self, a):
+        a = self._ct(a)
+        out = self._out(a.shape[0])
+        capi.check(self.lib.hg_negate(self.ctx.handle, self.id, _ptr(a), _ptr(out), a.shape[0]))
+        return out
+
+    def sum(self, a):
+        a = self._ct(a)
+        out = self._out(1)
+        capi.check(self.lib.hg_sum(self.ctx.handle, self.id, _ptr(a), a.shape[0], _ptr(out)))
+        return out
+
+    def to_mont(self, z):
+        z = self._ct(z)
+        out = self._out(z.shape[0])
+        capi.check(self.lib.hg_to_mont(self.ctx.handle, self.id, _ptr(z), _ptr(out), z.shape[0]))
+        return out
+
+    def from_mont(self, m):
+        m = self._ct(m)
+        out = self._out(m.shape[0])
+        capi.check(self.lib.hg_from_mont(self.ctx.handle, self.id, _ptr(m), _ptr(out), m.shape[0]))
+        return out

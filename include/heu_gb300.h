@@ -1,0 +1,139 @@
+/*
+ * heu_gb300 — C-ABI of a GB300 (sm_103a) Paillier engine with HEU
+ * `paillier_z` (ZPaillier, DJN-optimised Paillier) semantics.
+ *
+ * This is the device boundary a HEU schema adapter binds: plain pointers,
+ * sizes and int status codes, no C++ or torch types.  It replaces the
+ * reference's only device boundary, the CGBN C-ABI of `paillier_g`
+ * (heu/library/algorithms/paillier_gpu/gpulib/gpupaillier.h:46-91), and is
+ * called from the vectorized (span-of-pointers) SPI
+ * (heu/library/algorithms/clean_template/vector_encryptor.h:24-33,
+ *  vector_decryptor.h:25-31, vector_evaluator.h:24-66).
+ *
+ * Data formats (all little-endian 32-bit limbs, `k` = key bits = bitlen(n)):
+ *   ciphertext  S = k/16 limbs (k/4 bytes), stored in Montgomery form
+ *               c*R mod n^2 with R = 2^(32*S) — the representation HEU keeps
+ *               in paillier_z `Ciphertext::c_` (encryptor.cc:46-49).
+ *               hg_to_mont / hg_from_mont convert to and from the canonical
+ *               Z-form c in [0, n^2).
+ *   plaintext   int64_t, or (magnitude of k/32 limbs, sign byte) for the
+ *               full range |m| <= n/2 (public_key.h:50-54).
+ *   randomness  r of k/2 bits as k/64 limbs per ciphertext (the value
+ *               `BigInt::RandomExactBits(k/2)` draws in encryptor.cc:26-31),
+ *               injected by the caller so results are reproducible.
+ *
+ * Calls named hg_<op> take HOST pointers and are synchronous.  Calls named
+ * hg_dev_<op> take DEVICE pointers and are asynchronous on `stream` (a
+ * cudaStream_t passed as void*; NULL = the context's own stream).
+ *
+ * Every function returns HG_OK (0) or an HG_ERR_* code; hg_last_error()
+ * gives the message of the calling thread's last failure.
+ */
+#ifndef HEU_GB300_H_
+#define HEU_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HG_OK 0
+#define HG_ERR_INVALID 1        /* bad argument (null pointer, unknown key, size) */
+#define HG_ERR_CT_RANGE 2       /* a ciphertext >= n^2 (decryptor.cc:21-23) */
+#define HG_ERR_PT_RANGE 3       /* plaintext |m| > n/2 (encryptor.cc:38-40) */
+#define HG_ERR_NOMEM 4          /* device or host allocation failed */
+#define HG_ERR_CUDA 5           /* CUDA runtime error */
+#define HG_ERR_NOT_INVERTIBLE 6 /* gcd(c, n) != 1 in Negate/Sub/Mul(k<0) */
+#define HG_ERR_NO_SECRET 7      /* decrypt on a key loaded without p, q */
+#define HG_ERR_UNSUPPORTED 8    /* key size without a compiled variant */
+
+typedef struct hg_ctx hg_ctx;
+
+/* ---- context -------------------------------------------------------------
+ * Replaces gpu_setcard / gpu_release_context (gpupaillier.h:47-48, declared
+ * but never defined in the reference) and the per-call cudaSetDevice(0) +
+ * cudaMalloc/cudaFree of paillier.cu:565-632.                               */
+int hg_ctx_create(int device, hg_ctx** out);
+int hg_ctx_destroy(hg_ctx* ctx);
+const char* hg_last_error(void);
+int hg_device_sm_count(hg_ctx* ctx);
+
+/* ---- keys ----------------------------------------------------------------
+ * hg_keygen follows paillier_zahlen/key_generator.cc:26-60 on the host with
+ * every random draw taken from a seeded xoshiro256** stream (seed given) —
+ * the reference draws from yacl's RNG instead.  Outputs: n (k/32 limbs),
+ * p and q (k/64 limbs each), h_s = (-x^2)^n mod n^2 (k/16 limbs).          */
+int hg_keygen(uint32_t key_bits, uint64_t seed, uint32_t* n_out, uint32_t* p_out, uint32_t* q_out,
+              uint32_t* hs_out);
+
+/* Loads a key and uploads its precompute: Montgomery constants mod n^2
+ * (PublicKey::Init, public_key.cc:28-40), the fixed-base table of h_s
+ * powers with `table_window` bits per digit (0 = default; the reference's
+ * SetCacheTableDensity, public_key.cc:19-26, default 10), and, if p and q
+ * are given, the CRT constants of SecretKey::Init (secret_key.cc:19-43).
+ * p, q may be NULL for a public-key-only key.                              */
+int hg_key_load(hg_ctx* ctx, uint32_t key_bits, const uint32_t* n, const uint32_t* h_s, const uint32_t* p,
+                const uint32_t* q, int table_window, int* key_id);
+int hg_key_free(hg_ctx* ctx, int key_id);
+/* limbs of one ciphertext (S) and of one r value for a loaded key */
+int hg_key_shape(hg_ctx* ctx, int key_id, int* ct_limbs, int* r_limbs, int* pt_limbs);
+
+/* ---- encryption (replaces gpu_paillier_enc, gpupaillier.h:50-52) ---------
+ * c = (1 + m*n) * h_s^r mod n^2, output in Montgomery form
+ * (paillier_zahlen/encryptor.cc:36-56).                                   */
+int hg_encrypt(hg_ctx* ctx, int key_id, const int64_t* m, const uint32_t* r, uint32_t* ct_out, size_t count);
+int hg_encrypt_bn(hg_ctx* ctx, int key_id, const uint32_t* m_mag, const uint8_t* m_neg, const uint32_t* r,
+                  uint32_t* ct_out, size_t count);
+/* EncryptZero: h_s^r (encryptor.cc:33; vector_encryptor.h:28)              */
+int hg_encrypt_zero(hg_ctx* ctx, int key_id, const uint32_t* r, uint32_t* ct_out, size_t count);
+/* Randomize: c * h_s^r in place (evaluator.cc:25-28)                        */
+int hg_randomize(hg_ctx* ctx, int key_id, uint32_t* ct, const uint32_t* r, size_t count);
+
+/* ---- decryption (replaces gpu_paillier_dec, gpupaillier.h:53-55) ---------
+ * CRT over p^2 and q^2 (paillier_zahlen/decryptor.cc:32-53).  The int64
+ * form sets overflow[i] = 1 where the plaintext does not fit in int64 (the
+ * range check of numpy DecryptInRange, numpy/decryptor.cc:86-99).        */
+int hg_decrypt(hg_ctx* ctx, int key_id, const uint32_t* ct, int64_t* m_out, uint8_t* overflow, size_t count);
+int hg_decrypt_bn(hg_ctx* ctx, int key_id, const uint32_t* ct, uint32_t* m_mag, uint8_t* m_neg, size_t count);
+
+/* ---- evaluator (replaces gpu_paillier_e_add / e_add_const / sub_ct /
+ * sub_ctpt / sub_ptct / e_mul_const / e_inverse, gpupaillier.h:57-90) ---- */
+int hg_add(hg_ctx* ctx, int key_id, const uint32_t* a, const uint32_t* b, uint32_t* out, size_t count);
+int hg_add_plain(hg_ctx* ctx, int key_id, const uint32_t* a, const int64_t* p, uint32_t* out, size_t count);
+int hg_sub(hg_ctx* ctx, int key_id, const uint32_t* a, const uint32_t* b, uint32_t* out, size_t count);
+int hg_sub_plain(hg_ctx* ctx, int key_id, const uint32_t* a, const int64_t* p, uint32_t* out, size_t count);
+int hg_plain_sub(hg_ctx* ctx, int key_id, const int64_t* p, const uint32_t* a, uint32_t* out, size_t count);
+int hg_mul(hg_ctx* ctx, int key_id, const uint32_t* a, const int64_t* k, uint32_t* out, size_t count);
+int hg_negate(hg_ctx* ctx, int key_id, const uint32_t* a, uint32_t* out, size_t count);
+
+/* ---- heu.numpy reductions (numpy/evaluator.cc:355-373 Sum; the optional
+ * vectorized ReduceSum hook numpy MatMul detects, evaluator.cc:250-260) --- */
+int hg_sum(hg_ctx* ctx, int key_id, const uint32_t* a, size_t count, uint32_t* out);
+
+/* ---- representation ----------------------------------------------------- */
+int hg_to_mont(hg_ctx* ctx, int key_id, const uint32_t* z, uint32_t* mont, size_t count);
+int hg_from_mont(hg_ctx* ctx, int key_id, const uint32_t* mont, uint32_t* z, size_t count);
+
+/* ---- device-pointer forms (asynchronous on `stream`) --------------------
+ * Same semantics as the host forms above.  Range errors raised by kernels
+ * are collected per context; hg_dev_check(ctx) synchronises and reports
+ * them.  Negate / Sub / Mul with negative scalars synchronise `stream`
+ * once per call (the root of the inversion tree is inverted on the host). */
+int hg_dev_encrypt(hg_ctx* ctx, int key_id, const int64_t* m, const uint32_t* r, uint32_t* ct_out, size_t count,
+                   void* stream);
+int hg_dev_decrypt(hg_ctx* ctx, int key_id, const uint32_t* ct, int64_t* m_out, uint8_t* overflow, size_t count,
+                   void* stream);
+int hg_dev_add(hg_ctx* ctx, int key_id, const uint32_t* a, const uint32_t* b, uint32_t* out, size_t count,
+               void* stream);
+int hg_dev_mul(hg_ctx* ctx, int key_id, const uint32_t* a, const int64_t* k, uint32_t* out, size_t count,
+               void* stream);
+int hg_dev_sum(hg_ctx* ctx, int key_id, const uint32_t* a, size_t count, uint32_t* out, void* stream);
+int hg_dev_check(hg_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HEU_GB300_H_ */

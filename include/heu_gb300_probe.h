@@ -1,0 +1,22 @@
+/*
+ * Measurement probe shipped with the engine library.  It has no counterpart
+ * in the reference: it measures the device's integer multiply-accumulate
+ * throughput, the denominator of the Montgomery kernels' roofline.
+ */
+#ifndef HEU_GB300_PROBE_H_
+#define HEU_GB300_PROBE_H_
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* pattern 0: 32x32->64 MACs as mad.lo.cc/madc.hi.cc carry chains (the
+ * instruction pattern of the engine's Montgomery rows); pattern 1: MACs as
+ * mad.wide.u32 into 64-bit accumulators.  Returns 0 on success. */
+int hg_probe_mac_peak(int device, int pattern, double* macs_per_second, double* seconds);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HEU_GB300_PROBE_H_ */

@@ -1,0 +1,52 @@
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (runs the sm_103a engine)")
+    config.addinivalue_line("markers", "slow: longer CPU-only case")
+
+
+_KEY_CACHE = {}
+
+
+def oracle_key(bits, seed):
+    """(pk, sk) from the oracle's seeded key generation, cached per session."""
+    from oracle import paillier_z as pz
+
+    k = (bits, seed)
+    if k not in _KEY_CACHE:
+        _KEY_CACHE[k] = pz.keygen(bits, seed)
+    return _KEY_CACHE[k]
+
+
+@pytest.fixture(scope="session")
+def gpu_ctx():
+    import heu_gb300 as hg
+
+    ctx = hg.Context(0)
+    yield ctx
+    ctx.close()
+
+
+_GPU_KEYS = {}
+
+
+@pytest.fixture(scope="session")
+def gpu_key(gpu_ctx):
+    """Factory: loaded engine key for (bits, seed) plus the oracle key."""
+
+    def get(bits, seed=0, window=8):
+        k = (bits, seed, window)
+        if k not in _GPU_KEYS:
+            pk, sk = oracle_key(bits, seed)
+            _GPU_KEYS[k] = (gpu_ctx.load_key(bits, pk.n, pk.h_s, sk.p, sk.q, table_window=window), pk, sk)
+        return _GPU_KEYS[k]
+
+    return get

@@ -1,0 +1,265 @@
+"""Bit-exact parity of the sm_103a engine (through the C-ABI) with the
+paillier_z oracle on the same keys and the same injected r stream.
+
+Ciphertexts leave the engine in Montgomery form (HEU's representation); each
+test checks both that form (c*R mod n^2) and the canonical Z-form.
+"""
+
+import numpy as np
+import pytest
+
+import heu_gb300 as hg
+from heu_gb300 import capi
+from oracle import paillier_z as pz
+from oracle.prg import Prg
+
+pytestmark = pytest.mark.gpu
+
+KEYS = [(1024, 1), (2048, 0), (3072, 2)]
+I64_MIN, I64_MAX = -(2 ** 63), 2 ** 63 - 1
+EDGE_M = [0, 1, -1, 2, -2, 12345, -12345, 123, -123, 2 ** 31 - 1, -(2 ** 31), I64_MAX, I64_MIN, 6543212, -456]
+
+
+def rand_i64(prg, n, lo=I64_MIN, hi=I64_MAX + 1):
+    return [prg.int64_uniform(lo, hi) for _ in range(n)]
+
+
+def r_limbs(pk, rs, key):
+    return hg.ints_to_limbs(rs, key.r_limbs)
+
+
+def to_mont_limbs(pk, key, zs):
+    return hg.ints_to_limbs([pz.to_mont(pk, z) for z in zs], key.ct_limbs)
+
+
+def z_of(key, ct):
+    return hg.limbs_to_ints(key.from_mont(ct))
+
+
+def assert_ct_equal(pk, key, ct, expected_z, what):
+    got_m = hg.limbs_to_ints(ct)
+    exp_m = [pz.to_mont(pk, z) for z in expected_z]
+    bad = [i for i, (a, b) in enumerate(zip(got_m, exp_m)) if a != b]
+    assert not bad, f"{what}: {len(bad)} Montgomery-form mismatches, first at {bad[0]}"
+    got_z = z_of(key, ct)
+    bad = [i for i, (a, b) in enumerate(zip(got_z, expected_z)) if a != b]
+    assert not bad, f"{what}: {len(bad)} Z-form mismatches, first at {bad[0]}"
+
+
+@pytest.fixture(params=KEYS, ids=lambda k: f"k{k[0]}")
+def kk(request, gpu_key):
+    bits, seed = request.param
+    return gpu_key(bits, seed)
+
+
+def test_encrypt_matches_oracle(kk):
+    key, pk, sk = kk
+    prg = Prg(11)
+    ms = EDGE_M + rand_i64(prg, 49)
+    rs = pz.r_stream(7, len(ms), pk.key_size // 2)
+    ct = key.encrypt(np.array(ms, dtype=np.int64), r_limbs(pk, rs, key))
+    exp = [pz.encrypt(pk, m, r) for m, r in zip(ms, rs)]
+    assert_ct_equal(pk, key, ct, exp, "encrypt")
+
+
+def test_encrypt_edge_randomness(kk):
+    key, pk, sk = kk
+    top = (1 << (pk.key_size // 2)) - 1
+    rs = [0, 1, 2, top, top - 1, 1 << (pk.key_size // 2 - 1), 0x5555 << 100]
+    ms = [5] * len(rs)
+    ct = key.encrypt(np.array(ms, dtype=np.int64), r_limbs(pk, rs, key))
+    assert_ct_equal(pk, key, ct, [pz.encrypt(pk, m, r) for m, r in zip(ms, rs)], "encrypt edge r")
+
+
+def test_encrypt_zero_and_randomize(kk):
+    key, pk, sk = kk
+    rs = pz.r_stream(3, 9, pk.key_size // 2)
+    ez = key.encrypt_zero(r_limbs(pk, rs, key))
+    assert_ct_equal(pk, key, ez, [pz.encrypt_zero(pk, r) for r in rs], "encrypt_zero")
+    ms = list(range(-4, 5))
+    base_r = pz.r_stream(4, 9, pk.key_size // 2)
+    ct = key.encrypt(np.array(ms, dtype=np.int64), r_limbs(pk, base_r, key))
+    rr = key.randomize(ct, r_limbs(pk, rs, key))
+    exp = [pz.randomize(pk, pz.encrypt(pk, m, r0), r) for m, r0, r in zip(ms, base_r, rs)]
+    assert_ct_equal(pk, key, rr, exp, "randomize")
+
+
+def test_encrypt_bn_bounds(kk):
+    key, pk, sk = kk
+    nh = pk.n_half
+    ms = [nh, -nh, nh - 1, -(nh - 1), 2 ** 64 + 3, -(2 ** 100)]
+    rs = pz.r_stream(5, len(ms), pk.key_size // 2)
+    ct = key.encrypt_bn(ms, r_limbs(pk, rs, key))
+    assert_ct_equal(pk, key, ct, [pz.encrypt(pk, m, r) for m, r in zip(ms, rs)], "encrypt_bn")
+    assert key.decrypt_bn(ct) == ms
+    # paillier_test.cc:99-119: |m| = n/2 + 1 and n are rejected
+    for bad in (nh + 1, -(nh + 1), pk.n - 1):
+        with pytest.raises(hg.HgError) as ei:
+            key.encrypt_bn([bad], r_limbs(pk, rs[:1], key))
+        assert ei.value.code == capi.HG_ERR_PT_RANGE
+
+
+def test_decrypt_matches_oracle(kk):
+    key, pk, sk = kk
+    prg = Prg(12)
+    ms = EDGE_M + rand_i64(prg, 33)
+    rs = pz.r_stream(8, len(ms), pk.key_size // 2)
+    zs = [pz.encrypt(pk, m, r) for m, r in zip(ms, rs)]
+    ct = to_mont_limbs(pk, key, zs)
+    m, ovf = key.decrypt(ct)
+    assert ovf.sum() == 0
+    assert m.tolist() == ms
+    # big plaintexts through the bignum output
+    big = [pk.n_half, -pk.n_half, 2 ** 200 + 5, -(2 ** 77)]
+    rb = pz.r_stream(9, len(big), pk.key_size // 2)
+    ct = to_mont_limbs(pk, key, [pz.encrypt(pk, v, r) for v, r in zip(big, rb)])
+    assert key.decrypt_bn(ct) == big
+    m, ovf = key.decrypt(ct)
+    assert ovf.tolist() == [1, 1, 1, 1]
+
+
+def test_decrypt_arbitrary_residues(kk):
+    """Decrypt of residues that are not fresh encryptions (any c < n^2)."""
+    key, pk, sk = kk
+    prg = Prg(99)
+    zs = [prg.below(pk.n2) for _ in range(20)] + [1, pk.n2 - 1]
+    ct = to_mont_limbs(pk, key, zs)
+    got = key.decrypt_bn(ct)
+    assert got == [pz.decrypt(pk, sk, z) for z in zs]
+
+
+def test_add_sub_negate(kk):
+    key, pk, sk = kk
+    prg = Prg(13)
+    n = 40
+    ma = EDGE_M[:10] + rand_i64(prg, n - 10, -(2 ** 62), 2 ** 62)
+    mb = rand_i64(prg, n, -(2 ** 62), 2 ** 62)
+    ra = pz.r_stream(21, n, pk.key_size // 2)
+    rb = pz.r_stream(22, n, pk.key_size // 2)
+    za = [pz.encrypt(pk, m, r) for m, r in zip(ma, ra)]
+    zb = [pz.encrypt(pk, m, r) for m, r in zip(mb, rb)]
+    ca, cb = to_mont_limbs(pk, key, za), to_mont_limbs(pk, key, zb)
+    assert_ct_equal(pk, key, key.add(ca, cb), [pz.add(pk, a, b) for a, b in zip(za, zb)], "add")
+    assert_ct_equal(pk, key, key.negate(ca), [pz.negate(pk, a) for a in za], "negate")
+    assert_ct_equal(pk, key, key.sub(ca, cb), [pz.sub(pk, a, b) for a, b in zip(za, zb)], "sub")
+    m, _ = key.decrypt(key.sub(ca, cb))
+    assert m.tolist() == [a - b for a, b in zip(ma, mb)]
+
+
+def test_add_plain_variants(kk):
+    key, pk, sk = kk
+    prg = Prg(14)
+    ps = EDGE_M + rand_i64(prg, 17)
+    n = len(ps)
+    ms = rand_i64(prg, n, -(2 ** 40), 2 ** 40)
+    rs = pz.r_stream(23, n, pk.key_size // 2)
+    zs = [pz.encrypt(pk, m, r) for m, r in zip(ms, rs)]
+    c = to_mont_limbs(pk, key, zs)
+    p = np.array(ps, dtype=np.int64)
+    assert_ct_equal(pk, key, key.add_plain(c, p), [pz.add_plain(pk, z, q) for z, q in zip(zs, ps)], "add_plain")
+    assert_ct_equal(pk, key, key.sub_plain(c, p), [pz.sub_plain(pk, z, q) for z, q in zip(zs, ps)], "sub_plain")
+    assert_ct_equal(pk, key, key.plain_sub(p, c), [pz.sub_plain_ct(pk, q, z) for z, q in zip(zs, ps)],
+                    "plain_sub")
+
+
+def test_mul_scalars(kk):
+    key, pk, sk = kk
+    prg = Prg(15)
+    ks = [0, 1, -1, 2, -2, 3, -3, 2 ** 15 - 1, -(2 ** 15), 2 ** 31 - 1, -(2 ** 31), I64_MAX, I64_MIN,
+          I64_MIN + 1] + rand_i64(prg, 26)
+    n = len(ks)
+    ms = rand_i64(prg, n, -(2 ** 31), 2 ** 31)
+    rs = pz.r_stream(24, n, pk.key_size // 2)
+    zs = [pz.encrypt(pk, m, r) for m, r in zip(ms, rs)]
+    c = to_mont_limbs(pk, key, zs)
+    out = key.mul(c, np.array(ks, dtype=np.int64))
+    assert_ct_equal(pk, key, out, [pz.mul(pk, z, k) for z, k in zip(zs, ks)], "mul")
+
+
+def test_mul_all_positive_skips_inverse(kk):
+    key, pk, sk = kk
+    ks = [5, 7, 2 ** 40 + 1, 1, 0]
+    zs = [pz.encrypt(pk, m, r) for m, r in zip([3, -4, 5, 6, 7], pz.r_stream(25, 5, pk.key_size // 2))]
+    out = key.mul(to_mont_limbs(pk, key, zs), np.array(ks, dtype=np.int64))
+    assert_ct_equal(pk, key, out, [pz.mul(pk, z, k) for z, k in zip(zs, ks)], "mul positive")
+
+
+@pytest.mark.parametrize("count", [1, 2, 3, 17, 255, 256, 257, 900])
+def test_sum_counts(gpu_key, count):
+    key, pk, sk = gpu_key(2048, 0)
+    ms = list(range(count))
+    rs = pz.r_stream(30 + count, count, pk.key_size // 2)
+    zs = [pz.encrypt(pk, m, r) for m, r in zip(ms, rs)]
+    out = key.sum(to_mont_limbs(pk, key, zs))
+    assert_ct_equal(pk, key, out, [pz.sum_(pk, zs)], f"sum[{count}]")
+    # numpy_test.cc:111-120 (Sum of 0..899)
+    m, _ = key.decrypt(out)
+    assert int(m[0]) == count * (count - 1) // 2
+
+
+def test_ciphertext_range_rejected(kk):
+    key, pk, sk = kk
+    bad = hg.ints_to_limbs([pk.n2, pk.n2 + 5], key.ct_limbs)
+    good = to_mont_limbs(pk, key, [pz.encrypt(pk, 1, 1), pz.encrypt(pk, 2, 2)])
+    for fn in (lambda: key.add(bad, good), lambda: key.decrypt(bad), lambda: key.mul(bad, [2, 3]),
+               lambda: key.negate(bad), lambda: key.sum(bad)):
+        with pytest.raises(hg.HgError) as ei:
+            fn()
+        assert ei.value.code == capi.HG_ERR_CT_RANGE
+
+
+def test_montgomery_conversion_roundtrip(kk):
+    key, pk, sk = kk
+    prg = Prg(16)
+    zs = [prg.below(pk.n2) for _ in range(16)] + [0, 1, pk.n2 - 1]
+    zl = hg.ints_to_limbs(zs, key.ct_limbs)
+    mont = key.to_mont(zl)
+    assert hg.limbs_to_ints(mont) == [pz.to_mont(pk, z) for z in zs]
+    assert hg.limbs_to_ints(key.from_mont(mont)) == zs
+
+
+def test_table_window_does_not_change_results(gpu_ctx):
+    pk, sk = pz.keygen(1024, 1)
+    ms = [1, -2, 3, 2 ** 40]
+    rs = pz.r_stream(40, 4, pk.key_size // 2)
+    exp = [pz.encrypt(pk, m, r) for m, r in zip(ms, rs)]
+    for w in (1, 5, 10, 13):
+        key = gpu_ctx.load_key(1024, pk.n, pk.h_s, table_window=w)
+        ct = key.encrypt(np.array(ms, dtype=np.int64), hg.ints_to_limbs(rs, key.r_limbs))
+        assert_ct_equal(pk, key, ct, exp, f"window {w}")
+        with pytest.raises(hg.HgError) as ei:
+            key.decrypt(ct)
+        assert ei.value.code == capi.HG_ERR_NO_SECRET
+        key.free()
+
+
+def test_engine_keygen_matches_oracle_and_loads(gpu_ctx):
+    k = hg.keygen(2048, 0)
+    pk, sk = pz.keygen(2048, 0)
+    assert (k["n"], k["p"], k["q"], k["h_s"]) == (pk.n, sk.p, sk.q, pk.h_s)
+
+
+def test_config2_roundtrip_full_size(gpu_key):
+    """1,048,576 int64 plaintexts in [-2^40, 2^40): Encrypt -> Decrypt == m,
+    Add and Mul checked through decryption (size-independent properties)."""
+    key, pk, sk = gpu_key(2048, 0, 12)
+    n = 1 << 20
+    rng = np.random.default_rng(2)
+    m = rng.integers(-(2 ** 40), 2 ** 40, size=n, dtype=np.int64)
+    r = rng.integers(0, 2 ** 32, size=(n, key.r_limbs), dtype=np.uint64).astype(np.uint32)
+    ct = key.encrypt(m, r)
+    dm, ovf = key.decrypt(ct)
+    assert ovf.sum() == 0
+    assert np.array_equal(dm, m)
+    # a few spot checks against the oracle
+    for i in (0, 1, n // 2, n - 1):
+        rv = hg.limbs_to_ints(r[i:i + 1])[0]
+        assert hg.limbs_to_ints(key.from_mont(ct[i:i + 1]))[0] == pz.encrypt(pk, int(m[i]), rv)
+    s = key.add(ct, ct[::-1].copy())
+    dm, _ = key.decrypt(s)
+    assert np.array_equal(dm, m + m[::-1])
+    k = rng.integers(-(2 ** 15), 2 ** 15, size=n, dtype=np.int64)
+    mm = key.mul(ct, k)
+    dm, ovf = key.decrypt(mm)
+    assert ovf.sum() == 0
+    assert np.array_equal(dm, m * k)
