@@ -1,0 +1,448 @@
+#!/usr/bin/env python3
+"""Paillier-2048 throughput on one GB300 (HEU paillier_z semantics).
+
+Workload (one step): one 2048-bit key (seed 0); 1,048,576 int64 plaintexts
+m ~ U[-2^40, 2^40) with injected 1024-bit r; Encrypt (fixed-base h_s^r),
+ciphertext Add (ct + ct'), scalar Mul by 64-bit k ~ U[-2^63, 2^63), CRT
+Decrypt of the sums.  value = 4 * 2^20 ops per step / step time, with every
+input already resident in HBM (512 MiB of ciphertexts per array, larger than
+the 129 MB L2, so no flush is needed between steps).  e2e repeats the step
+through the host-pointer C-ABI (hg_encrypt / hg_add / hg_mul / hg_decrypt)
+with pinned host buffers, so every copy is inside the timed region.
+
+--impl reference times the paillier_z CPU path (the oracle's C restatement;
+HEU itself needs Bazel + yacl and does not build here) on all host cores,
+each step a bounded sample of the same workload.
+"""
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+KEY_BITS = 2048
+KEY_SEED = 0
+M_BITS = 40
+METRIC = "Paillier-2048 ops/s (enc/dec/mul/sum) and serve p99 ms, batched vs plain GPU"
+UNIT = "ops/s"
+WORKLOAD = "config2: 2048-bit key, 2^20 int64 m~U[-2^40,2^40), enc+add+mul(64-bit k)+CRT dec per step"
+
+
+def mm_macs(limbs):
+    """Montgomery multiplication cost in 32x32 MACs: 2s^2 + s."""
+    return 2 * limbs * limbs + limbs
+
+
+def decrypt_macs(key_bits, wd=6):
+    """Algorithmic MACs of one CRT decryption (two (k/2)-bit exponentiations
+    mod p^2, q^2 with sliding windows of wd bits, plus 3 MM for L and CRT)."""
+    h = key_bits // 2
+    sp = key_bits // 32
+    steps = (h - 1) + -(-h // (wd + 1)) + 2 ** (wd - 1)
+    return 2 * steps * mm_macs(sp) + 3 * mm_macs(sp)
+
+
+def encrypt_macs(key_bits, w):
+    return (-(-(key_bits // 2) // w) + 2) * mm_macs(key_bits // 16)
+
+
+def mul_macs(key_bits, ks, wm=4):
+    tot = 0
+    for k in ks:
+        b = abs(int(k)).bit_length()
+        if b == 0:
+            continue
+        tot += (b - 1 + -(-b // (wm + 1)) + 2 ** (wm - 1) + 2)
+    return tot * mm_macs(key_bits // 16)
+
+
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.out = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.out, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.out.close()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ---------------------------------------------------------------------------
+def cpu_sample(seconds_hint=10.0, threads=None):
+    """Time the paillier_z C restatement on a bounded sample of the workload.
+
+    Returns per-op rates (ops/s) and the step-equivalent rate for the
+    enc+add+mul+dec mix."""
+    import numpy as np
+
+    from oracle import cref
+    from oracle import paillier_z as pz
+
+    threads = threads or os.cpu_count() or 1
+    pk, sk = pz.keygen(KEY_BITS, KEY_SEED)
+    ck = cref.CKey(KEY_BITS, pk, sk, window=10)
+    rng = np.random.default_rng(7)
+    n_fast = 512 * threads
+    n_dec = 96 * threads
+    m = rng.integers(-(2 ** M_BITS), 2 ** M_BITS, size=n_fast, dtype=np.int64)
+    r = rng.integers(0, 2 ** 63, size=(n_fast, ck.r_limbs), dtype=np.int64).astype(np.uint64) * 2 + 1
+    k = rng.integers(-(2 ** 63), 2 ** 63 - 1, size=n_fast, dtype=np.int64)
+    rates = {}
+    t = time.perf_counter()
+    ct = ck.encrypt(m, r, threads)
+    rates["encrypt"] = n_fast / (time.perf_counter() - t)
+    t = time.perf_counter()
+    cs = ck.add(ct, ct[::-1].copy(), threads)
+    rates["add"] = n_fast / (time.perf_counter() - t)
+    n_mul = 128 * threads
+    t = time.perf_counter()
+    ck.mul(ct[:n_mul].copy(), k[:n_mul], threads)
+    rates["mul"] = n_mul / (time.perf_counter() - t)
+    t = time.perf_counter()
+    d, _ = ck.decrypt(cs[:n_dec].copy(), threads)
+    rates["decrypt"] = n_dec / (time.perf_counter() - t)
+    assert np.array_equal(d, (m + m[::-1])[:n_dec]), "CPU baseline decrypt mismatch"
+    step_rate = 4.0 / sum(1.0 / rates[o] for o in ("encrypt", "add", "mul", "decrypt"))
+    sample = (f"{n_fast} encrypt+add, {n_mul} mul (64-bit k), {n_dec} CRT decrypt on 2048-bit key; "
+              "step-equivalent rate = 4/(sum 1/rate_op)")
+    return rates, step_rate, threads, sample
+
+
+def reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    import numpy as np
+
+    from oracle import cref
+    from oracle import paillier_z as pz
+
+    threads = os.cpu_count() or 1
+    pk, sk = pz.keygen(KEY_BITS, KEY_SEED)
+    ck = cref.CKey(KEY_BITS, pk, sk, window=10)
+    ns = 64 * threads
+    rng = np.random.default_rng(11)
+    m = rng.integers(-(2 ** M_BITS), 2 ** M_BITS, size=ns, dtype=np.int64)
+    m2 = rng.integers(-(2 ** M_BITS), 2 ** M_BITS, size=ns, dtype=np.int64)
+    r = rng.integers(0, 2 ** 63, size=(ns, ck.r_limbs), dtype=np.int64).astype(np.uint64) * 2 + 1
+    k = rng.integers(-(2 ** 63), 2 ** 63 - 1, size=ns, dtype=np.int64)
+    ct2 = ck.encrypt(m2, r, threads)
+
+    def step():
+        ct = ck.encrypt(m, r, threads)
+        cs = ck.add(ct, ct2, threads)
+        ck.mul(ct, k, threads)
+        d, _ = ck.decrypt(cs, threads)
+        return d
+
+    for _ in range(args.warmup):
+        d = step()
+    assert np.array_equal(d, m + m2)
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    dt = time.perf_counter() - t
+    value = 4 * ns * args.steps / dt
+    sample = f"{ns} elements per step (enc+add+mul+dec), paillier_z C restatement, {threads} threads"
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+        "data": "synthetic", "config": {"workload": WORKLOAD, "sample_elements_per_step": ns},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+def ours_arm(args):
+    import numpy as np
+    import torch
+
+    import heu_gb300 as hg
+    from heu_gb300 import capi
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    lib = capi.load()
+    n = args.n
+    kp = hg.keygen(KEY_BITS, KEY_SEED)
+    ctx = hg.Context(local)
+    key = ctx.load_key(KEY_BITS, kp["n"], kp["h_s"], kp["p"], kp["q"], table_window=args.window)
+    S, RL = key.ct_limbs, key.r_limbs
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(1000 + rank)
+    m = torch.randint(-(2 ** M_BITS), 2 ** M_BITS, (n,), dtype=torch.int64, device=dev, generator=gen)
+    m2 = torch.randint(-(2 ** M_BITS), 2 ** M_BITS, (n,), dtype=torch.int64, device=dev, generator=gen)
+    r = torch.randint(-(2 ** 31), 2 ** 31, (n, RL), dtype=torch.int32, device=dev, generator=gen)
+    r2 = torch.randint(-(2 ** 31), 2 ** 31, (n, RL), dtype=torch.int32, device=dev, generator=gen)
+    kk = torch.randint(-(2 ** 63), 2 ** 63 - 1, (n,), dtype=torch.int64, device=dev, generator=gen)
+    ct = torch.empty((n, S), dtype=torch.int32, device=dev)
+    ct2 = torch.empty_like(ct)
+    cs = torch.empty_like(ct)
+    cm = torch.empty_like(ct)
+    d = torch.empty((n,), dtype=torch.int64, device=dev)
+    ovf = torch.empty((n,), dtype=torch.uint8, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    h = ctx.handle
+
+    def P(x):
+        return ctypes.c_void_p(x.data_ptr())
+
+    with torch.cuda.stream(stream):
+        capi.check(lib.hg_dev_encrypt(h, key.id, P(m2), P(r2), P(ct2), n, sp))
+    torch.cuda.synchronize()
+
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(5)] for _ in range(args.steps)]
+
+    ops = args.ops
+    if "add" not in ops:
+        cs.copy_(ct2)  # decrypt then reads the setup ciphertexts (plaintexts m2)
+
+    def step(e=None):
+        with torch.cuda.stream(stream):
+            if e:
+                e[0].record(stream)
+            if "encrypt" in ops:
+                capi.check(lib.hg_dev_encrypt(h, key.id, P(m), P(r), P(ct), n, sp))
+            if e:
+                e[1].record(stream)
+            if "add" in ops:
+                capi.check(lib.hg_dev_add(h, key.id, P(ct), P(ct2), P(cs), n, sp))
+            if e:
+                e[2].record(stream)
+            if "mul" in ops:
+                capi.check(lib.hg_dev_mul(h, key.id, P(ct), P(kk), P(cm), n, sp))
+            if e:
+                e[3].record(stream)
+            if "decrypt" in ops:
+                capi.check(lib.hg_dev_decrypt(h, key.id, P(cs), P(d), P(ovf), n, sp))
+            if e:
+                e[4].record(stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    capi.check(lib.hg_dev_check(h))
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clk = ClockSampler(local)
+    clk.start()
+    launches0 = capi.launch_count()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for i in range(args.steps):
+        step(ev[i])
+    t1.record(stream)
+    torch.cuda.synchronize()
+    launches = capi.launch_count() - launches0
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    elapsed = t0.elapsed_time(t1) / 1e3
+    names = ("encrypt", "add", "mul", "decrypt")
+    op_s = {nm: sum(ev[i][j].elapsed_time(ev[i][j + 1]) for i in range(args.steps)) / 1e3
+            for j, nm in enumerate(names)}
+    if dist:
+        t = torch.tensor([elapsed], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t.item())
+    capi.check(lib.hg_dev_check(h))
+    # correctness of the timed outputs
+    if "decrypt" in ops:
+        assert int(ovf.sum().item()) == 0
+        want = (m + m2) if ("add" in ops and "encrypt" in ops) else m2
+        if "add" in ops or "encrypt" not in ops:
+            assert torch.equal(d, want), "decrypt mismatch"
+    if "mul" in ops and "encrypt" in ops:
+        idx = [0, 1, n // 3, n - 1]
+        cm_h = cm[idx].cpu().numpy().view(np.uint32)
+        got = key.decrypt_bn(cm_h)
+        mh, kh = m[idx].cpu().tolist(), kk[idx].cpu().tolist()
+        assert got == [a * b for a, b in zip(mh, kh)], "mul spot check mismatch"
+
+    value = len(ops) * n * world * args.steps / elapsed
+    per_op = {nm: n * args.steps / op_s[nm] for nm in names if nm in ops}
+    macs_dec = decrypt_macs(KEY_BITS) * n
+    dec_avg = op_s["decrypt"] / args.steps
+    achieved = macs_dec / dec_avg / 1e12 if "decrypt" in ops else None
+    peak_chain = capi.mac_peak(local, 0) / 1e12
+    peak_wide = capi.mac_peak(local, 1) / 1e12
+    peak = max(peak_chain, peak_wide)
+    k_host = kk.cpu().numpy()
+    work = {
+        "encrypt": encrypt_macs(KEY_BITS, args.window) * n,
+        "add": mm_macs(KEY_BITS // 16) * n,
+        "mul": mul_macs(KEY_BITS, k_host[: 1 << 14]) * (n / min(n, 1 << 14)),
+        "decrypt": macs_dec,
+    }
+    roof_ops = {nm: work[nm] / (op_s[nm] / args.steps) / 1e12 for nm in names if nm in ops}
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        try:
+            tj = json.load(open(tpath))
+            traffic = tj.get("decrypt_bytes_per_ciphertext", None)
+            if traffic is not None:
+                traffic = traffic * n
+        except (OSError, ValueError):
+            traffic = None
+
+    # ---- e2e through the host-pointer C-ABI ------------------------------
+    e2e = None
+    if not args.no_e2e:
+        pin = dict(pin_memory=True)
+        m_h = m.cpu().pin_memory()
+        r_h = r.cpu().pin_memory()
+        k_h = kk.cpu().pin_memory()
+        ct2_h = ct2.cpu().pin_memory()
+        ct_h = torch.empty((n, S), dtype=torch.int32, **pin)
+        cs_h = torch.empty((n, S), dtype=torch.int32, **pin)
+        cm_hh = torch.empty((n, S), dtype=torch.int32, **pin)
+        d_h = torch.empty((n,), dtype=torch.int64, **pin)
+        o_h = torch.empty((n,), dtype=torch.uint8, **pin)
+
+        def e2e_step():
+            capi.check(lib.hg_encrypt(h, key.id, P(m_h), P(r_h), P(ct_h), n))
+            capi.check(lib.hg_add(h, key.id, P(ct_h), P(ct2_h), P(cs_h), n))
+            capi.check(lib.hg_mul(h, key.id, P(ct_h), P(k_h), P(cm_hh), n))
+            capi.check(lib.hg_decrypt(h, key.id, P(cs_h), P(d_h), P(o_h), n))
+
+        e2e_step()
+        if dist:
+            dist.barrier()
+        t = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            e2e_step()
+        e2e_dt = time.perf_counter() - t
+        if dist:
+            tt = torch.tensor([e2e_dt], device=dev, dtype=torch.float64)
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            e2e_dt = float(tt.item())
+        assert torch.equal(d_h, (m + m2).cpu()), "e2e decrypt mismatch"
+        assert len(ops) == 4, "e2e runs the full step"
+        cb = S * 4
+        h2d = n * (8 + RL * 4) + n * 2 * cb + n * (cb + 8) + n * cb
+        d2h = n * cb * 3 + n * 9
+        e2e = {"value": 4 * n * world * args.e2e_steps / e2e_dt, "unit": UNIT, "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "steps": args.e2e_steps,
+               "api": "hg_encrypt/hg_add/hg_mul/hg_decrypt (host pointers, pinned)"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        rates, step_rate, cores, sample = cpu_sample()
+        cpu = {"value": step_rate, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample,
+               "per_op": rates}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "key_bits": KEY_BITS, "batch": n, "table_window": args.window,
+                       "l2": "inputs larger than L2 (512 MiB per ciphertext array); no flush",
+                       "parallelism": f"replicas x{world}"},
+            "per_op_ops_per_s": per_op,
+            "roofline": {"bound": "imad", "kernel": "decrypt (CRT, k_decrypt)", "achieved": achieved,
+                         "peak": peak, "unit": "TMAC/s", "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                         "peak_source": "measured live: hg_probe_mac_peak (best of mad.wide / carry-chain "
+                                        "patterns); MEASURED_PEAKS.json has no integer figure",
+                         "peak_chain_pattern": peak_chain, "peak_wide_pattern": peak_wide,
+                         "per_op_tmacs": roof_ops},
+            "e2e": e2e,
+            "cpu_baseline": cpu,
+            "gpu_launches": launches,
+            "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    ctx.close()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=1 << 20)
+    ap.add_argument("--window", type=int, default=16)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--ops", default="encrypt,add,mul,decrypt",
+                    help="subset of the step's ops (for profiling one kernel)")
+    args = ap.parse_args()
+    args.ops = [o for o in args.ops.split(",") if o]
+    if args.impl == "reference":
+        return reference_arm(args)
+    return ours_arm(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

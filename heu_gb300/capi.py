@@ -69,6 +69,7 @@ SIGNATURES = {
     "hg_dev_sum": [_P, _I, _P, _SZ, _P, _P],
     "hg_dev_check": [_P],
     "hg_probe_mac_peak": [_I, _I, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)],
+    "hg_probe_launch_count": [ctypes.POINTER(_U64)],
 }
 
 _lib = None
@@ -121,6 +122,13 @@ def declared_symbols():
         text = open(header_path).read()
         names.update(re.findall(r"^\s*(?:int|const char\*)\s+(hg_\w+)\s*\(", text, re.M))
     return sorted(names)
+
+
+def launch_count():
+    """Engine kernels launched by this process so far."""
+    v = _U64()
+    check(load().hg_probe_launch_count(ctypes.byref(v)))
+    return v.value
 
 
 def mac_peak(device=0, pattern=0):

@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "../../include/heu_gb300.h"
+#include "../../include/heu_gb300_probe.h"
 #include "host_bn.hpp"
 #include "paillier_kernels.cuh"
 
@@ -949,6 +950,12 @@ int hg_dev_sum(hg_ctx* ctx, int key_id, const uint32_t* a, size_t count, uint32_
     core_sum(*k, w, a, count, out);
     return HG_OK;
   });
+}
+
+int hg_probe_launch_count(uint64_t* out) {
+  if (!out) return HG_ERR_INVALID;
+  *out = hg::launch_count();
+  return HG_OK;
 }
 
 int hg_dev_check(hg_ctx* ctx) {

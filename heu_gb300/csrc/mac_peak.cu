@@ -84,7 +84,7 @@ extern "C" int hg_probe_mac_peak(int device, int pattern, double* macs_per_secon
   };
   launch();  // warm-up
   cudaEventRecord(e0);
-  const int reps = 5;
+  const int reps = 40;  // about half a second of sustained load
   for (int i = 0; i < reps; ++i) launch();
   cudaEventRecord(e1);
   cudaError_t err = cudaEventSynchronize(e1);

@@ -6,6 +6,7 @@
 // (square vs multiply, which table entry) only change the data a uniform
 // Montgomery multiplication consumes.
 #include <algorithm>
+#include <atomic>
 
 #include "mont.cuh"
 #include "paillier_kernels.cuh"
@@ -751,6 +752,13 @@ __global__ void __launch_bounds__(kBlock) k_table_level(KeyConst kc, uint32_t* _
 
 bool supported_limbs(int S) { return S == 64 || S == 128 || S == 192; }
 
+static std::atomic<uint64_t> g_launches{0};
+uint64_t launch_count() { return g_launches.load(); }
+static inline cudaError_t counted() {
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  return cudaGetLastError();
+}
+
 static inline unsigned blocks_for(size_t instances, int tpi) {
   const size_t ipb = kBlock / tpi;
   return (unsigned)((instances + ipb - 1) / ipb);
@@ -807,14 +815,14 @@ cudaError_t launch_encrypt(int S, const KeyConst& kc, EncMode mode, const int64_
     const unsigned gb = (unsigned)std::min((size_t)need, (size_t)(grid > 0 ? (unsigned)grid : need));
     k_encrypt<TPI, L><<<gb, kBlock, 0, st>>>(kc, mode, m, m_mag, m_neg, r, ct_in, out, count, err);
   });
-  return cudaGetLastError();
+  return counted();
 }
 
 cudaError_t launch_add(int S, const KeyConst& kc, const uint32_t* a, const uint32_t* b, uint32_t* out,
                        size_t count, uint32_t* err, cudaStream_t st) {
   if (count == 0) return cudaSuccess;
   HG_DISPATCH_S(S, k_add<TPI, L><<<blocks_for(count, TPI), kBlock, 0, st>>>(kc, a, b, out, count, err));
-  return cudaGetLastError();
+  return counted();
 }
 
 cudaError_t launch_add_plain(int S, const KeyConst& kc, const uint32_t* a, const int64_t* p, int neg_p,
@@ -822,7 +830,7 @@ cudaError_t launch_add_plain(int S, const KeyConst& kc, const uint32_t* a, const
   if (count == 0) return cudaSuccess;
   HG_DISPATCH_S(S, k_add_plain<TPI, L><<<blocks_for(count, TPI), kBlock, 0, st>>>(kc, a, p, neg_p, out,
                                                                                    count, err));
-  return cudaGetLastError();
+  return counted();
 }
 
 cudaError_t launch_mul(int S, const KeyConst& kc, const uint32_t* a, const int64_t* k, uint32_t* out,
@@ -833,7 +841,7 @@ cudaError_t launch_mul(int S, const KeyConst& kc, const uint32_t* a, const int64
     const unsigned gb = (unsigned)std::min((size_t)need, (size_t)grid);
     k_mul<TPI, L><<<gb, kBlock, 0, st>>>(kc, a, k, out, count, scratch, wm, err);
   });
-  return cudaGetLastError();
+  return counted();
 }
 
 cudaError_t launch_decrypt(int Sp, const KeyConst& kc, const SecConst& sc, const uint32_t* ct, size_t count,
@@ -847,7 +855,7 @@ cudaError_t launch_decrypt(int Sp, const KeyConst& kc, const SecConst& sc, const
     k_decrypt<TP, LP><<<gb, kBlock, 0, st>>>(kc, sc, ct, count, out_i64, out_ovf, out_mag, out_neg, scratch,
                                               err);
   });
-  return cudaGetLastError();
+  return counted();
 }
 
 cudaError_t launch_convert(int S, const KeyConst& kc, const uint32_t* in, uint32_t* out, size_t count,
@@ -855,7 +863,7 @@ cudaError_t launch_convert(int S, const KeyConst& kc, const uint32_t* in, uint32
   if (count == 0) return cudaSuccess;
   HG_DISPATCH_S(S, k_convert<TPI, L><<<blocks_for(count, TPI), kBlock, 0, st>>>(kc, in, out, count, to_mont,
                                                                                  err));
-  return cudaGetLastError();
+  return counted();
 }
 
 cudaError_t launch_reduce(int S, const KeyConst& kc, const uint32_t* in, size_t count, int chunk,
@@ -864,47 +872,47 @@ cudaError_t launch_reduce(int S, const KeyConst& kc, const uint32_t* in, size_t 
   const size_t out_count = (count + chunk - 1) / chunk;
   HG_DISPATCH_S(S, k_reduce<TPI, L><<<blocks_for(out_count, TPI), kBlock, 0, st>>>(kc, in, count, chunk, out,
                                                                                     out_count, err));
-  return cudaGetLastError();
+  return counted();
 }
 
 cudaError_t launch_tree_leaves(int S, const KeyConst& kc, const uint32_t* in, const int64_t* sel, size_t count,
                                uint32_t* leaves, size_t padded, uint32_t* err, cudaStream_t st) {
   HG_DISPATCH_S(S, k_tree_leaves<TPI, L><<<blocks_for(padded, TPI), kBlock, 0, st>>>(kc, in, sel, count,
                                                                                       leaves, padded, err));
-  return cudaGetLastError();
+  return counted();
 }
 
 cudaError_t launch_tree_up(int S, const KeyConst& kc, const uint32_t* lower, uint32_t* upper, size_t upper_count,
                            cudaStream_t st) {
   HG_DISPATCH_S(S, k_tree_up<TPI, L><<<blocks_for(upper_count, TPI), kBlock, 0, st>>>(kc, lower, upper,
                                                                                        upper_count));
-  return cudaGetLastError();
+  return counted();
 }
 
 cudaError_t launch_tree_down(int S, const KeyConst& kc, uint32_t* lower, const uint32_t* upper_inv,
                              size_t upper_count, cudaStream_t st) {
   HG_DISPATCH_S(S, k_tree_down<TPI, L><<<blocks_for(upper_count, TPI), kBlock, 0, st>>>(kc, lower, upper_inv,
                                                                                          upper_count));
-  return cudaGetLastError();
+  return counted();
 }
 
 cudaError_t launch_tree_apply(int S, const KeyConst& kc, const uint32_t* in, const int64_t* sel,
                               const uint32_t* leaves_inv, uint32_t* out, size_t count, cudaStream_t st) {
   HG_DISPATCH_S(S, k_tree_apply<TPI, L><<<blocks_for(count, TPI), kBlock, 0, st>>>(kc, in, sel, leaves_inv,
                                                                                     out, count));
-  return cudaGetLastError();
+  return counted();
 }
 
 cudaError_t launch_root_fix(int S, const KeyConst& kc, const uint32_t* root_inv_z, uint32_t* root_slot,
                             cudaStream_t st) {
   HG_DISPATCH_S(S, k_root_fix<TPI, L><<<1, 32, 0, st>>>(kc, root_inv_z, root_slot));
-  return cudaGetLastError();
+  return counted();
 }
 
 cudaError_t launch_table_bases(int S, const KeyConst& kc, const uint32_t* hs_mont, uint32_t* bases,
                                cudaStream_t st) {
   HG_DISPATCH_S(S, k_table_bases<TPI, L><<<1, 32, 0, st>>>(kc, hs_mont, bases));
-  return cudaGetLastError();
+  return counted();
 }
 
 cudaError_t launch_table_level(int S, const KeyConst& kc, uint32_t* table, const uint32_t* bases, int level,
@@ -920,7 +928,7 @@ cudaError_t launch_table_level(int S, const KeyConst& kc, uint32_t* table, const
     total = (hi - lo + 1) * (size_t)kc.npos;
   }
   HG_DISPATCH_S(S, k_table_level<TPI, L><<<blocks_for(total, TPI), kBlock, 0, st>>>(kc, table, bases, level));
-  return cudaGetLastError();
+  return counted();
 }
 
 }  // namespace hg

@@ -97,5 +97,6 @@ int instances_per_block(int S);
 int units_per_block_decrypt(int Sp);
 
 bool supported_limbs(int S);
+uint64_t launch_count();  // kernels launched by this process so far
 
 }  // namespace hg

@@ -6,6 +6,8 @@
 #ifndef HEU_GB300_PROBE_H_
 #define HEU_GB300_PROBE_H_
 
+#include <stdint.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -14,6 +16,9 @@ extern "C" {
  * instruction pattern of the engine's Montgomery rows); pattern 1: MACs as
  * mad.wide.u32 into 64-bit accumulators.  Returns 0 on success. */
 int hg_probe_mac_peak(int device, int pattern, double* macs_per_second, double* seconds);
+
+/* Number of engine kernels this process has launched so far. */
+int hg_probe_launch_count(uint64_t* out);
 
 #ifdef __cplusplus
 }
