@@ -67,6 +67,7 @@ SIGNATURES = {
     "hg_dev_add": [_P, _I, _P, _P, _P, _SZ, _P],
     "hg_dev_mul": [_P, _I, _P, _P, _P, _SZ, _P],
     "hg_dev_sum": [_P, _I, _P, _SZ, _P, _P],
+    "hg_dev_sum_noalloc": [_P, _I, _P, _SZ, _P, _P],
     "hg_dev_check": [_P],
     "hg_probe_mac_peak": [_I, _I, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)],
     "hg_probe_launch_count": [ctypes.POINTER(_U64)],

@@ -15,6 +15,7 @@
 
 #include "../../include/heu_gb300.h"
 #include "../../include/heu_gb300_probe.h"
+#include "engine_internal.hpp"
 #include "host_bn.hpp"
 #include "paillier_kernels.cuh"
 
@@ -978,3 +979,21 @@ int hg_dev_check(hg_ctx* ctx) {
 }
 
 }  // extern "C"
+
+namespace hg {
+
+int key_view(hg_ctx* ctx, int key_id, KeyConst* kc, int* S, int* device, cudaStream_t* own_stream) {
+  if (!ctx) return HG_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  auto it = ctx->keys.find(key_id);
+  if (it == ctx->keys.end()) return HG_ERR_INVALID;
+  *kc = it->second->kc;
+  *S = it->second->S;
+  *device = ctx->device;
+  *own_stream = ctx->lanes[0]->stream;
+  return HG_OK;
+}
+
+void set_last_error(const char* msg) { g_last_error = msg; }
+
+}  // namespace hg

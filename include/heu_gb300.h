@@ -130,6 +130,20 @@ int hg_dev_add(hg_ctx* ctx, int key_id, const uint32_t* a, const uint32_t* b, ui
 int hg_dev_mul(hg_ctx* ctx, int key_id, const uint32_t* a, const int64_t* k, uint32_t* out, size_t count,
                void* stream);
 int hg_dev_sum(hg_ctx* ctx, int key_id, const uint32_t* a, size_t count, uint32_t* out, void* stream);
+/* Allocation-free Sum.  No counterpart in the reference.  For callers that
+ * cannot call cudaMalloc (device memory owned by another allocator or
+ * reserved up front): same result as hg_dev_sum, but the partial products
+ * live in a fixed 16 MiB device array inside the library, which every GPU
+ * that loads the library holds until the process exits.  count is limited
+ * to 128 * floor((16 MiB - 256) / (8 * S)) ciphertexts (S = limbs per
+ * ciphertext: 4,194,176 / 2,097,024 / 1,398,016 for 1024 / 2048 / 3072-bit
+ * keys); larger counts are rejected with HG_ERR_INVALID before any work.
+ * Allocates no device memory and calls no cudaMalloc / cudaFree.  The first
+ * call on a device resolves the array's address (cudaGetSymbolAddress), so
+ * make that first call before any stream capture.  Calls share the array:
+ * calls that overlap on the GPU race.  Synchronises `stream` before
+ * returning, so range errors come back as HG_ERR_CT_RANGE.                */
+int hg_dev_sum_noalloc(hg_ctx* ctx, int key_id, const uint32_t* a, size_t count, uint32_t* out, void* stream);
 int hg_dev_check(hg_ctx* ctx);
 
 #ifdef __cplusplus
