@@ -69,6 +69,10 @@ SIGNATURES = {
     "hg_dev_sum": [_P, _I, _P, _SZ, _P, _P],
     "hg_dev_sum_noalloc": [_P, _I, _P, _SZ, _P, _P],
     "hg_dev_check": [_P],
+    "hg_bucket_sum": [_P, _I, _P, _SZ, _SZ, _P, _SZ, _I, _I, _P],
+    "hg_dev_bucket_sum": [_P, _I, _P, _SZ, _SZ, _P, _SZ, _I, _I, _P, _P],
+    "hg_matmul": [_P, _I, _P, _SZ, _SZ, _P, _SZ, _P],
+    "hg_dev_matmul": [_P, _I, _P, _SZ, _SZ, _P, _SZ, _P, _P],
     "hg_probe_mac_peak": [_I, _I, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)],
     "hg_probe_launch_count": [ctypes.POINTER(_U64)],
 }

@@ -157,6 +157,8 @@ struct Work {
   bool own_stream = false;
   DevBuf io[6];
   DevBuf scratch, tree, red[2], zbuf;
+  DevBuf seg_cnt, seg_offs[3], seg_cursor, seg_idx, seg_nch, seg_part[2];
+  DevBuf mm_tables, mm_masks, mm_prod;
   DevBuf err;
   PinBuf pin_root, pin_err;
   ~Work() {
@@ -217,6 +219,7 @@ void reset_err(Work& w) { cuda_check(cudaMemsetAsync(w.errp(), 0, sizeof(uint32_
 
 void raise_err_bits(uint32_t bits) {
   if (bits & hg::kErrCtRange) fail(HG_ERR_CT_RANGE, "Invalid ciphertext: value >= n^2");
+  if (bits & hg::kErrBinRange) fail(HG_ERR_INVALID, "order map holds a bin id >= bucket_num");
   if (bits & hg::kErrPtRange) fail(HG_ERR_PT_RANGE, "message number out of range: |m| > n/2");
   if (bits & hg::kErrNotInvertible) fail(HG_ERR_NOT_INVERTIBLE, "ciphertext not invertible mod n^2");
 }
@@ -339,6 +342,101 @@ void core_sum(KeyRec& k, Work& w, const uint32_t* a, size_t count, uint32_t* out
     n = outn;
     which ^= 1;
   }
+}
+
+
+// FeatureWiseBucketSum (numpy/evaluator.cc:378-458) over device arrays.
+void core_bucket_sum(KeyRec& k, Work& w, const uint32_t* x, size_t rows, size_t cols, const uint8_t* om, int F,
+                     int B, int cumsum, uint32_t* out) {
+  if (rows == 0 || cols == 0) fail(HG_ERR_INVALID, "you cannot sum an empty tensor");
+  if (F <= 0 || B <= 0 || B > 256) fail(HG_ERR_INVALID, "features must be > 0 and 0 < bucket_num <= 256");
+  const size_t S = (size_t)k.S;
+  const int nseg = F * B;
+  if ((size_t)F * rows >= (1ull << 32)) fail(HG_ERR_INVALID, "features * rows must be < 2^32");
+  uint32_t* cnt = w.seg_cnt.ensure<uint32_t>((size_t)nseg * 4);
+  uint32_t* offs0 = w.seg_offs[0].ensure<uint32_t>(((size_t)nseg + 1) * 4);
+  uint32_t* cursor = w.seg_cursor.ensure<uint32_t>((size_t)nseg * 4);
+  uint32_t* idx = w.seg_idx.ensure<uint32_t>((size_t)F * rows * 4);
+  uint32_t* nch = w.seg_nch.ensure<uint32_t>((size_t)nseg * 4);
+  cuda_check(hg::launch_bin_sort(om, rows, F, B, cnt, offs0, cursor, idx, w.errp(), w.stream), "bin sort");
+  const int C = 64;
+  for (size_t col = 0; col < cols; ++col) {
+    const uint32_t* vals = x;
+    size_t stride = cols, voff = col;
+    const uint32_t* vidx = idx;
+    const uint32_t* offs_in = offs0;
+    size_t total_in = (size_t)F * rows;  // elements across all segments
+    size_t max_len = rows;
+    int which = 0;
+    do {
+      const size_t upper = total_in / C + (size_t)nseg + 1;
+      uint32_t* part = w.seg_part[which].ensure<uint32_t>(upper * S * 4);
+      uint32_t* offs_out = w.seg_offs[1 + which].ensure<uint32_t>(((size_t)nseg + 1) * 4);
+      cuda_check(hg::launch_seg_level(k.S, k.kc, vals, stride, voff, vidx, offs_in, nseg, C, nch, offs_out, part,
+                                      upper, w.errp(), w.stream),
+                 "segment level");
+      vals = part;
+      stride = 1;
+      voff = 0;
+      vidx = nullptr;
+      offs_in = offs_out;
+      total_in = upper;
+      max_len = (max_len + C - 1) / C;
+      which ^= 1;
+    } while (max_len > 1);
+    cuda_check(hg::launch_seg_finalize(k.S, vals, offs_in, nseg, k.kc.R1, out, cols, col, w.stream), "finalize");
+    if (cumsum) cuda_check(hg::launch_bucket_cumsum(k.S, k.kc, out, F, B, cols, col, w.stream), "cumsum");
+  }
+}
+
+// numpy MatMul of ciphertexts x (M x K) by int64 plaintexts y (K x N, host).
+void core_matmul(KeyRec& k, Work& w, const uint32_t* x, size_t M, size_t K, const int64_t* y, size_t N,
+                 uint32_t* out) {
+  if (M == 0 || K == 0 || N == 0) fail(HG_ERR_INVALID, "HEU does not support empty tensor currently");
+  if (K > (1u << 20) || N > (1u << 20)) fail(HG_ERR_INVALID, "matmul dimension too large");
+  int64_t ymin = y[0], ymax = y[0];
+  for (size_t i = 1; i < K * N; ++i) {
+    ymin = std::min(ymin, y[i]);
+    ymax = std::max(ymax, y[i]);
+  }
+  // shift to y' = y + o >= 0; undo with (prod_k x(i,k))^-o per row
+  const uint64_t o = ymin < 0 ? (uint64_t)0 - (uint64_t)ymin : 0;
+  const uint64_t ymax_s = (uint64_t)ymax + o;
+  int P = 1;
+  while (P < 64 && (ymax_s >> P) != 0) ++P;
+  const int nch = (int)((K + 7) / 8);
+  std::vector<uint8_t> hm((size_t)N * P * nch, 0);
+  for (size_t j = 0; j < N; ++j)
+    for (int plane = 0; plane < P; ++plane)
+      for (int c = 0; c < nch; ++c) {
+        uint8_t mk = 0;
+        for (int b = 0; b < 8; ++b) {
+          const size_t kk = (size_t)c * 8 + b;
+          if (kk < K && ((((uint64_t)y[kk * N + j] + o) >> plane) & 1ull)) mk |= (uint8_t)(1u << b);
+        }
+        hm[((size_t)j * P + plane) * nch + c] = mk;
+      }
+  uint8_t* dmask = w.mm_masks.ensure<uint8_t>(hm.size());
+  cuda_check(cudaMemcpyAsync(dmask, hm.data(), hm.size(), cudaMemcpyHostToDevice, w.stream), "H2D masks");
+  const size_t per_row = hg::subset_table_bytes_per_row(k.S, (int)K);
+  const size_t budget = (size_t)8 << 30;
+  const size_t Rb = std::max<size_t>(1, std::min(M, budget / per_row));
+  uint32_t* T = w.mm_tables.ensure<uint32_t>(Rb * per_row);
+  uint32_t* prod = w.mm_prod.ensure<uint32_t>(Rb * (size_t)k.S * 4);
+  for (size_t r0 = 0; r0 < M; r0 += Rb) {
+    const size_t rows = std::min(Rb, M - r0);
+    cuda_check(hg::launch_subset_tables(k.S, k.kc, x, r0, rows, (int)K, T, w.errp(), w.stream), "subset tables");
+    cuda_check(hg::launch_matmul_planes(k.S, k.kc, T, dmask, r0, rows, (int)N, P, (int)K, out, w.stream),
+               "matmul planes");
+    if (o > 0) {
+      cuda_check(hg::launch_row_products(k.S, k.kc, T, rows, (int)K, prod, w.stream), "row products");
+      core_inverse(k, w, prod, nullptr, prod, rows);
+      cuda_check(hg::launch_pow_shared(k.S, k.kc, prod, rows, o, w.stream), "row power");
+      cuda_check(hg::launch_scale_rows(k.S, k.kc, out, prod, r0, rows, (int)N, w.stream), "scale rows");
+    }
+  }
+  // keep the host mask array alive until its copy has run
+  cuda_check(cudaStreamSynchronize(w.stream), "stream sync");
 }
 
 int load_key(hg_ctx* ctx, uint32_t key_bits, const uint32_t* n_l, const uint32_t* hs_l, const uint32_t* p_l,
@@ -949,6 +1047,67 @@ int hg_dev_sum(hg_ctx* ctx, int key_id, const uint32_t* a, size_t count, uint32_
     if (count == 0) fail(HG_ERR_INVALID, "you cannot sum an empty tensor");
     HG_DEV_PROLOGUE
     core_sum(*k, w, a, count, out);
+    return HG_OK;
+  });
+}
+
+
+int hg_bucket_sum(hg_ctx* ctx, int key_id, const uint32_t* x, size_t rows, size_t cols, const uint8_t* order_map,
+                  size_t features, int bucket_num, int cumsum, uint32_t* out) {
+  return guarded([&] {
+    if (!x || !order_map || !out) fail(HG_ERR_INVALID, "null argument");
+    const size_t count = rows * cols;
+    if (count == 0) fail(HG_ERR_INVALID, "you cannot sum an empty tensor");
+    HG_HOST_PROLOGUE
+    auto* dx = w.io[0].ensure<uint32_t>(count * cb);
+    auto* dom = w.io[1].ensure<uint8_t>(rows * features);
+    const size_t outn = features * (size_t)bucket_num * cols;
+    auto* dout = w.io[2].ensure<uint32_t>(outn * cb);
+    h2d(dx, x, count * cb, w);
+    h2d(dom, order_map, rows * features, w);
+    core_bucket_sum(*k, w, dx, rows, cols, dom, (int)features, bucket_num, cumsum, dout);
+    d2h(out, dout, outn * cb, w);
+    finish(w);
+    return HG_OK;
+  });
+}
+
+int hg_dev_bucket_sum(hg_ctx* ctx, int key_id, const uint32_t* x, size_t rows, size_t cols, const uint8_t* order_map,
+                      size_t features, int bucket_num, int cumsum, uint32_t* out, void* stream) {
+  return guarded([&] {
+    const size_t count = rows * cols;
+    if (count == 0) fail(HG_ERR_INVALID, "you cannot sum an empty tensor");
+    HG_DEV_PROLOGUE
+    core_bucket_sum(*k, w, x, rows, cols, order_map, (int)features, bucket_num, cumsum, out);
+    return HG_OK;
+  });
+}
+
+int hg_matmul(hg_ctx* ctx, int key_id, const uint32_t* x, size_t M, size_t K, const int64_t* y, size_t N,
+              uint32_t* out) {
+  return guarded([&] {
+    if (!x || !y || !out) fail(HG_ERR_INVALID, "null argument");
+    const size_t count = M * K;
+    if (count == 0 || N == 0) fail(HG_ERR_INVALID, "HEU does not support empty tensor currently");
+    HG_HOST_PROLOGUE
+    auto* dx = w.io[0].ensure<uint32_t>(count * cb);
+    auto* dout = w.io[1].ensure<uint32_t>(M * N * cb);
+    h2d(dx, x, count * cb, w);
+    core_matmul(*k, w, dx, M, K, y, N, dout);
+    d2h(out, dout, M * N * cb, w);
+    finish(w);
+    return HG_OK;
+  });
+}
+
+int hg_dev_matmul(hg_ctx* ctx, int key_id, const uint32_t* x, size_t M, size_t K, const int64_t* y, size_t N,
+                  uint32_t* out, void* stream) {
+  return guarded([&] {
+    if (!y) fail(HG_ERR_INVALID, "null argument");
+    const size_t count = M * K;
+    if (count == 0 || N == 0) fail(HG_ERR_INVALID, "HEU does not support empty tensor currently");
+    HG_DEV_PROLOGUE
+    core_matmul(*k, w, x, M, K, y, N, out);
     return HG_OK;
   });
 }

@@ -1,7 +1,7 @@
 // Integer multiply-accumulate throughput probe (the roofline denominator for
 // the Montgomery kernels).  Pure register work, no memory traffic:
-//   pattern 0: 32x32->64 MACs as carry chains of mad.lo.cc / madc.hi.cc,
-//              exactly the row pattern of mont.cuh (2 instructions per MAC);
+//   pattern 0: 32x32->64 MACs as carry chains of mad.lo.cc / madc.hi.cc
+//              (2 instructions per MAC);
 //   pattern 1: 32x32->64 MACs as mad.wide.u32 into 64-bit accumulators.
 // Reported as MACs per second over the whole device.
 #include <cuda_runtime.h>
@@ -15,6 +15,21 @@ namespace {
 
 constexpr int kRowL = 16;
 
+// One row of carry-chained 32x32->64 MACs: T (+ carry words) += x * y.
+__device__ __forceinline__ void row_chain(uint32_t (&T)[kRowL], uint32_t& c0, uint32_t& c1,
+                                          const uint32_t (&x)[kRowL], uint32_t y) {
+  T[0] = hg::mad_lo_cc(x[0], y, T[0]);
+#pragma unroll
+  for (int j = 1; j < kRowL; ++j) T[j] = hg::madc_lo_cc(x[j], y, T[j]);
+  c0 = hg::addc_cc(c0, 0u);
+  c1 = hg::addc(c1, 0u);
+  T[1] = hg::mad_hi_cc(x[0], y, T[1]);
+#pragma unroll
+  for (int j = 1; j < kRowL - 1; ++j) T[j + 1] = hg::madc_hi_cc(x[j], y, T[j + 1]);
+  c0 = hg::madc_hi_cc(x[kRowL - 1], y, c0);
+  c1 = hg::addc(c1, 0u);
+}
+
 __global__ void __launch_bounds__(256) k_mac_chain(uint32_t* sink, uint32_t seed, int iters) {
   uint32_t x[kRowL], T[kRowL];
 #pragma unroll
@@ -27,7 +42,7 @@ __global__ void __launch_bounds__(256) k_mac_chain(uint32_t* sink, uint32_t seed
   for (int it = 0; it < iters; ++it) {
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
-      hg::row_mac<kRowL>(T, c0, c1, x, y);
+      row_chain(T, c0, c1, x, y);
       y ^= T[r];
     }
   }

@@ -12,6 +12,7 @@ enum : uint32_t {
   kErrCtRange = 1u,      // a ciphertext >= n^2 reached a kernel
   kErrNotInvertible = 2u,
   kErrPtRange = 4u,      // a plaintext with |m| > n/2
+  kErrBinRange = 8u,     // an order-map bin id >= bucket_num
 };
 
 // Public-key constants for arithmetic mod N = n^2 with R = 2^(32*S).
@@ -88,6 +89,29 @@ cudaError_t launch_table_bases(int S, const KeyConst& kc, const uint32_t* hs_mon
                                cudaStream_t st);
 cudaError_t launch_table_level(int S, const KeyConst& kc, uint32_t* table, const uint32_t* bases, int level,
                                cudaStream_t st);
+
+// FeatureWiseBucketSum building blocks (reduce_kernels.cu)
+cudaError_t launch_bin_sort(const uint8_t* om, size_t rows, int F, int B, uint32_t* cnt, uint32_t* offs,
+                            uint32_t* cursor, uint32_t* idx, uint32_t* err, cudaStream_t st);
+cudaError_t launch_seg_level(int S, const KeyConst& kc, const uint32_t* vals, size_t stride, size_t voff,
+                             const uint32_t* idx, const uint32_t* offs_in, int nseg, int C, uint32_t* nch,
+                             uint32_t* offs_out, uint32_t* out, size_t upper, uint32_t* err, cudaStream_t st);
+cudaError_t launch_seg_finalize(int S, const uint32_t* vals, const uint32_t* offs, int nseg, const uint32_t* R1,
+                                uint32_t* out, size_t ostride, size_t ooff, cudaStream_t st);
+cudaError_t launch_bucket_cumsum(int S, const KeyConst& kc, uint32_t* out, int F, int B, size_t ostride,
+                                 size_t ooff, cudaStream_t st);
+
+// MatMul building blocks (matmul_kernels.cu)
+cudaError_t launch_subset_tables(int S, const KeyConst& kc, const uint32_t* x, size_t r0, size_t rows, int K,
+                                 uint32_t* T, uint32_t* err, cudaStream_t st);
+cudaError_t launch_matmul_planes(int S, const KeyConst& kc, const uint32_t* T, const uint8_t* masks, size_t r0,
+                                 size_t rows, int Ncols, int P, int K, uint32_t* out, cudaStream_t st);
+cudaError_t launch_row_products(int S, const KeyConst& kc, const uint32_t* T, size_t rows, int K, uint32_t* prod,
+                                cudaStream_t st);
+cudaError_t launch_pow_shared(int S, const KeyConst& kc, uint32_t* v, size_t count, uint64_t e, cudaStream_t st);
+cudaError_t launch_scale_rows(int S, const KeyConst& kc, uint32_t* out, const uint32_t* q, size_t r0, size_t rows,
+                              int Ncols, cudaStream_t st);
+size_t subset_table_bytes_per_row(int S, int K);
 
 // Occupancy-derived grid sizes (blocks) for the persistent kernels.
 int resident_blocks_encrypt(int S);

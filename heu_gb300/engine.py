@@ -226,3 +226,32 @@ class Key:
         out = self._out(m.shape[0])
         capi.check(self.lib.hg_from_mont(self.ctx.handle, self.id, _ptr(m), _ptr(out), m.shape[0]))
         return out
+
+    # -- heu.numpy reductions ----------------------------------------------
+    def bucket_sum(self, x, order_map, bucket_num, cumsum=False):
+        """FeatureWiseBucketSum: x (rows, cols, S) or (rows, S) ciphertexts,
+        order_map (rows, features) uint8 bin ids -> (features*bucket_num, cols, S)."""
+        x = np.ascontiguousarray(x, dtype=np.uint32)
+        if x.ndim == 2:
+            x = x.reshape(x.shape[0], 1, x.shape[1])
+        rows, cols = x.shape[0], x.shape[1]
+        om = np.ascontiguousarray(order_map, dtype=np.uint8)
+        if om.ndim != 2 or om.shape[0] != rows:
+            raise ValueError("order map and x should have same number of rows.")
+        feats = om.shape[1]
+        out = np.empty((feats * bucket_num, cols, self.ct_limbs), dtype=np.uint32)
+        capi.check(self.lib.hg_bucket_sum(self.ctx.handle, self.id, _ptr(x), rows, cols, _ptr(om), feats,
+                                          bucket_num, 1 if cumsum else 0, _ptr(out)))
+        return out
+
+    def matmul(self, x, y):
+        """Ciphertext matrix x (M, K, S) times int64 matrix y (K, N) -> (M, N, S)."""
+        x = np.ascontiguousarray(x, dtype=np.uint32)
+        y = np.ascontiguousarray(y, dtype=np.int64)
+        M, K = x.shape[0], x.shape[1]
+        if y.shape[0] != K:
+            raise ValueError("dimension mismatch for matmul")
+        N = y.shape[1]
+        out = np.empty((M, N, self.ct_limbs), dtype=np.uint32)
+        capi.check(self.lib.hg_matmul(self.ctx.handle, self.id, _ptr(x), M, K, _ptr(y), N, _ptr(out)))
+        return out

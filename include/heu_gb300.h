@@ -112,6 +112,23 @@ int hg_negate(hg_ctx* ctx, int key_id, const uint32_t* a, uint32_t* out, size_t 
  * vectorized ReduceSum hook numpy MatMul detects, evaluator.cc:250-260) --- */
 int hg_sum(hg_ctx* ctx, int key_id, const uint32_t* a, size_t count, uint32_t* out);
 
+/* FeatureWiseBucketSum (numpy/evaluator.cc:378-458; pylib
+ * extension_functions.cc:80-98): x is rows x cols ciphertexts (row-major),
+ * order_map rows x features bin ids (row-major), out (features*bucket_num) x
+ * cols; row f*bucket_num+b of out is the product of x(i, col) over rows with
+ * order_map(i, f) == b, or the Montgomery identity (GetZero,
+ * numpy/evaluator.h:84-87) for an empty bucket; cumsum != 0 turns bucket b
+ * into the product of buckets 0..b (evaluator.cc:444-449).  The reference's
+ * order map is int8 (numpy/evaluator.h:21-23) and cannot hold bin ids >= 128;
+ * this one is uint8 with bucket_num <= 256.                                 */
+int hg_bucket_sum(hg_ctx* ctx, int key_id, const uint32_t* x, size_t rows, size_t cols, const uint8_t* order_map,
+                  size_t features, int bucket_num, int cumsum, uint32_t* out);
+/* MatMul of ciphertexts x (M x K, row-major) by int64 plaintexts y (K x N,
+ * row-major): out(i,j) = prod_k x(i,k)^y(k,j) (numpy/evaluator.cc:208-353,
+ * the vectorized Mul + ReduceSum path).  pt x ct is the transpose.        */
+int hg_matmul(hg_ctx* ctx, int key_id, const uint32_t* x, size_t M, size_t K, const int64_t* y, size_t N,
+              uint32_t* out);
+
 /* ---- representation ----------------------------------------------------- */
 int hg_to_mont(hg_ctx* ctx, int key_id, const uint32_t* z, uint32_t* mont, size_t count);
 int hg_from_mont(hg_ctx* ctx, int key_id, const uint32_t* mont, uint32_t* z, size_t count);
@@ -144,6 +161,12 @@ int hg_dev_sum(hg_ctx* ctx, int key_id, const uint32_t* a, size_t count, uint32_
  * calls that overlap on the GPU race.  Synchronises `stream` before
  * returning, so range errors come back as HG_ERR_CT_RANGE.                */
 int hg_dev_sum_noalloc(hg_ctx* ctx, int key_id, const uint32_t* a, size_t count, uint32_t* out, void* stream);
+int hg_dev_bucket_sum(hg_ctx* ctx, int key_id, const uint32_t* x, size_t rows, size_t cols, const uint8_t* order_map,
+                      size_t features, int bucket_num, int cumsum, uint32_t* out, void* stream);
+/* y stays in HOST memory (it is small and is turned into bit-plane masks on
+ * the host); x and out are device pointers. */
+int hg_dev_matmul(hg_ctx* ctx, int key_id, const uint32_t* x, size_t M, size_t K, const int64_t* y, size_t N,
+                  uint32_t* out, void* stream);
 int hg_dev_check(hg_ctx* ctx);
 
 #ifdef __cplusplus

@@ -12,9 +12,9 @@
 extern "C" {
 #endif
 
-/* pattern 0: 32x32->64 MACs as mad.lo.cc/madc.hi.cc carry chains (the
- * instruction pattern of the engine's Montgomery rows); pattern 1: MACs as
- * mad.wide.u32 into 64-bit accumulators.  Returns 0 on success. */
+/* pattern 0: 32x32->64 MACs as mad.lo.cc/madc.hi.cc carry chains; pattern 1:
+ * MACs as mad.wide.u32 into 64-bit accumulators (the device's fastest integer
+ * MAC form, the roofline peak).  Returns 0 on success. */
 int hg_probe_mac_peak(int device, int pattern, double* macs_per_second, double* seconds);
 
 /* Number of engine kernels this process has launched so far. */

@@ -1,0 +1,137 @@
+"""heu.numpy reductions on the engine: FeatureWiseBucketSum and MatMul,
+bit-exact against the oracle on small shapes and checked through decryption
+at the full config-3 sizes."""
+
+import numpy as np
+import pytest
+
+import heu_gb300 as hg
+from heu_gb300 import capi
+from oracle import paillier_z as pz
+
+pytestmark = pytest.mark.gpu
+
+
+def enc_matrix(key, pk, vals, seed):
+    flat = [int(v) for v in np.asarray(vals).reshape(-1)]
+    rs = pz.r_stream(seed, len(flat), pk.key_size // 2)
+    zs = [pz.encrypt(pk, m, r) for m, r in zip(flat, rs)]
+    ct = key.encrypt(np.array(flat, dtype=np.int64), hg.ints_to_limbs(rs, key.r_limbs))
+    return ct, zs
+
+
+def zform(key, ct):
+    return hg.limbs_to_ints(key.from_mont(ct.reshape(-1, key.ct_limbs)))
+
+
+@pytest.mark.parametrize("cumsum", [False, True])
+def test_bucket_sum_matches_oracle(gpu_key, cumsum):
+    key, pk, sk = gpu_key(1024, 1)
+    rng = np.random.default_rng(3)
+    rows, cols, feats, buckets = 300, 2, 5, 7
+    vals = rng.integers(-1000, 1000, size=(rows, cols))
+    om = rng.integers(0, buckets, size=(rows, feats)).astype(np.uint8)
+    om[:, 4] = 3  # one feature with every row in one bucket (others empty)
+    ct, zs = enc_matrix(key, pk, vals, 51)
+    out = key.bucket_sum(ct.reshape(rows, cols, -1), om, buckets, cumsum=cumsum)
+    x = [[zs[i * cols + c] for c in range(cols)] for i in range(rows)]
+    exp = pz.bucket_sum(pk, x, om.tolist(), buckets, cumsum=cumsum)
+    got = zform(key, out)
+    assert got == [v for row in exp for v in row]
+
+
+def test_bin_sum_literal_case(gpu_key):
+    """numpy_test.cc:167-183: rows 2..4 of a 5x2 matrix of 0..9, 10 features,
+    5 buckets; result (2, 0) decrypts to 4."""
+    key, pk, sk = gpu_key(2048, 0)
+    order_map = np.array([[1, 3, 2, 2, 3, 3, 0, 0, 0, 0],
+                          [2, 3, 0, 1, 0, 1, 2, 3, 0, 1],
+                          [2, 1, 1, 1, 0, 2, 0, 1, 1, 1],
+                          [3, 2, 2, 0, 0, 1, 1, 1, 2, 3],
+                          [0, 0, 2, 2, 3, 3, 0, 3, 2, 2]], dtype=np.uint8)
+    m = np.arange(10).reshape(5, 2)
+    sub = [2, 3, 4]
+    ct, _ = enc_matrix(key, pk, m[sub], 52)
+    out = key.bucket_sum(ct.reshape(3, 2, -1), order_map[sub], 5)
+    d, _ = key.decrypt(out.reshape(-1, key.ct_limbs))
+    d = d.reshape(50, 2)
+    assert d[2, 0] == 4
+
+
+def test_bucket_sum_rejects_bad_bins(gpu_key):
+    key, pk, sk = gpu_key(1024, 1)
+    ct, _ = enc_matrix(key, pk, [1, 2, 3], 53)
+    om = np.array([[0], [9], [1]], dtype=np.uint8)
+    with pytest.raises(hg.HgError) as ei:
+        key.bucket_sum(ct, om, 4)
+    assert ei.value.code == capi.HG_ERR_INVALID
+
+
+@pytest.mark.parametrize("nkm", [(1, 1, 1), (1, 1, 20), (10, 1, 1), (1, 100, 1), (10, 1, 20), (20, 30, 1),
+                                 (1, 100, 3), (2, 3, 4), (10, 30, 20)])
+def test_matmul_shapes_match_oracle(gpu_key, nkm):
+    """matmul_test.cc:21-68 shapes (x from 10, y from 5), ct x pt."""
+    key, pk, sk = gpu_key(1024, 1)
+    n, k, m = nkm
+    x = np.arange(10, 10 + n * k, dtype=np.int64).reshape(n, k)
+    y = np.arange(5, 5 + k * m, dtype=np.int64).reshape(k, m)
+    ct, zs = enc_matrix(key, pk, x, 54)
+    out = key.matmul(ct.reshape(n, k, -1), y)
+    d, ovf = key.decrypt(out.reshape(-1, key.ct_limbs))
+    assert ovf.sum() == 0 and np.array_equal(d.reshape(n, m), x @ y)
+    if n * k * m <= 200:
+        cx = [[zs[i * k + j] for j in range(k)] for i in range(n)]
+        assert zform(key, out) == [v for row in pz.matmul(pk, cx, y.tolist()) for v in row]
+
+
+def test_matmul_signed_and_extreme_scalars(gpu_key):
+    key, pk, sk = gpu_key(2048, 0)
+    rng = np.random.default_rng(9)
+    x = rng.integers(-(2 ** 20), 2 ** 20, size=(3, 11))
+    y = rng.integers(-(2 ** 15), 2 ** 15, size=(11, 4))
+    y[0, 0], y[1, 1], y[2, 2] = 0, -1, 2 ** 40
+    ct, zs = enc_matrix(key, pk, x, 55)
+    out = key.matmul(ct.reshape(3, 11, -1), y)
+    cx = [[zs[i * 11 + j] for j in range(11)] for i in range(3)]
+    assert zform(key, out) == [v for row in pz.matmul(pk, cx, y.tolist()) for v in row]
+    yz = np.zeros((11, 2), dtype=np.int64)
+    out = key.matmul(ct.reshape(3, 11, -1), yz)
+    assert zform(key, out) == [1] * 6
+    yb = np.full((11, 1), -(2 ** 62), dtype=np.int64)
+    out = key.matmul(ct.reshape(3, 11, -1), yb)
+    assert zform(key, out) == [v for row in pz.matmul(pk, cx, yb.tolist()) for v in row]
+
+
+def test_config3_bucket_sum_full_size(gpu_key):
+    """2^20 fixed-point gradients (scale 2^20), 64 features x 256 buckets:
+    decrypted bucket sums equal the integer bucket sums."""
+    key, pk, sk = gpu_key(2048, 0, 12)
+    rows, feats, buckets = 1 << 20, 64, 256
+    rng = np.random.default_rng(31)
+    g = np.round(rng.standard_normal(rows) * (1 << 20)).astype(np.int64)
+    r = rng.integers(0, 2 ** 32, size=(rows, key.r_limbs), dtype=np.uint64).astype(np.uint32)
+    ct = key.encrypt(g, r)
+    om = rng.integers(0, buckets, size=(rows, feats)).astype(np.uint8)
+    out = key.bucket_sum(ct, om, buckets)
+    d, ovf = key.decrypt(out.reshape(-1, key.ct_limbs))
+    assert ovf.sum() == 0
+    exact = np.zeros((feats, buckets), dtype=np.int64)
+    for f in range(feats):
+        np.add.at(exact[f], om[:, f], g)
+    assert np.array_equal(d.reshape(feats, buckets), exact)
+
+
+def test_config3_matmul_full_size(gpu_key):
+    """4096 x 256 ciphertexts @ 256 x 64 int32 in [-2^15, 2^15): decrypted
+    result equals the int64 matmul."""
+    key, pk, sk = gpu_key(2048, 0, 12)
+    M, K, N = 4096, 256, 64
+    rng = np.random.default_rng(32)
+    x = np.round(rng.standard_normal((M, K)) * (1 << 20)).astype(np.int64)
+    y = rng.integers(-(2 ** 15), 2 ** 15, size=(K, N), dtype=np.int64)
+    r = rng.integers(0, 2 ** 32, size=(M * K, key.r_limbs), dtype=np.uint64).astype(np.uint32)
+    ct = key.encrypt(x.reshape(-1), r)
+    out = key.matmul(ct.reshape(M, K, -1), y)
+    d, ovf = key.decrypt(out.reshape(-1, key.ct_limbs))
+    assert ovf.sum() == 0
+    assert np.array_equal(d.reshape(M, N), x @ y)
