@@ -227,6 +227,11 @@ def ours_arm(args):
     kp = hg.keygen(KEY_BITS, KEY_SEED)
     ctx = hg.Context(local)
     key = ctx.load_key(KEY_BITS, kp["n"], kp["h_s"], kp["p"], kp["q"], table_window=args.window)
+    tuned = None
+    if not args.no_tune:
+        from heu_gb300 import autotune
+
+        tuned, _ = autotune.tune(key, calib=131072)
     S, RL = key.ct_limbs, key.r_limbs
     gen = torch.Generator(device=dev)
     gen.manual_seed(1000 + rank)
@@ -402,6 +407,7 @@ def ours_arm(args):
             "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
             "config": {"workload": WORKLOAD, "key_bits": KEY_BITS, "batch": n, "table_window": args.window,
+                       "autotuned": tuned,
                        "l2": "inputs larger than L2 (512 MiB per ciphertext array); no flush",
                        "parallelism": f"replicas x{world}"},
             "per_op_ops_per_s": per_op,
@@ -424,6 +430,248 @@ def ours_arm(args):
     return 0
 
 
+# ---------------------------------------------------------------------------
+def _load_keys(ctx, spec, tune):
+    """spec: list of (bits, seed, table_window) -> loaded keys (tuned if asked)."""
+    import heu_gb300 as hg
+    from heu_gb300 import autotune
+
+    keys = []
+    for bits, seed, w in spec:
+        kp = hg.keygen(bits, seed)
+        key = ctx.load_key(bits, kp["n"], kp["h_s"], kp["p"], kp["q"], table_window=w)
+        if tune:
+            autotune.tune(key, calib=131072)
+        keys.append(key)
+    return keys
+
+
+def c4_arm(args):
+    """Config 4: 64 uneven jobs over 1024/2048/3072-bit keys (lengths
+    log-uniform in [16, 262144], op mix 40% encrypt / 30% mul / 20% add / 10%
+    decrypt, int64 plaintexts and scalars uniform), run as one persistent
+    launch replayed from a CUDA graph, against the plain per-call kernels."""
+    import numpy as np
+    import torch
+
+    import heu_gb300 as hg
+    from heu_gb300 import capi
+    from heu_gb300.batch import ADD, DECRYPT, ENCRYPT, MUL
+
+    dev = torch.device("cuda", 0)
+    ctx = hg.Context(0)
+    lib, h = ctx.lib, ctx.handle
+    keys = _load_keys(ctx, [(1024, 1, 16), (2048, 0, 16), (3072, 2, 14)], not args.no_tune)
+    rng = np.random.default_rng(4)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(44)
+    ops_p = [0.4, 0.3, 0.2, 0.1]
+    op_codes = [ENCRYPT, MUL, ADD, DECRYPT]
+    jobs = []
+    total = 0
+    for _ in range(64):
+        key = keys[int(rng.integers(3))]
+        n = int(np.floor(np.exp(rng.uniform(np.log(16), np.log(262144)))))
+        op = op_codes[int(rng.choice(4, p=ops_p))]
+        S, RL = key.ct_limbs, key.r_limbs
+        m = torch.randint(-(2 ** 63), 2 ** 63 - 1, (n,), dtype=torch.int64, device=dev, generator=gen)
+        r = torch.randint(-(2 ** 31), 2 ** 31, (n, RL), dtype=torch.int32, device=dev, generator=gen)
+        base = torch.empty((n, S), dtype=torch.int32, device=dev)
+        capi.check(lib.hg_dev_encrypt(h, key.id, ctypes.c_void_p(m.data_ptr()), ctypes.c_void_p(r.data_ptr()),
+                                      ctypes.c_void_p(base.data_ptr()), n, None))
+        j = dict(key=key, n=n, op=op, m=m, r=r, base=base)
+        if op == MUL:
+            j["k"] = torch.randint(-(2 ** 63), 2 ** 63 - 1, (n,), dtype=torch.int64, device=dev, generator=gen)
+        if op == ADD:
+            j["other"] = base.roll(1, 0).contiguous()
+        if op == DECRYPT:
+            j["out_p"] = torch.empty((n,), dtype=torch.int64, device=dev)
+            j["out_b"] = torch.empty((n,), dtype=torch.int64, device=dev)
+            j["ovf"] = torch.empty((n,), dtype=torch.uint8, device=dev)
+        else:
+            j["out_p"] = torch.empty((n, S), dtype=torch.int32, device=dev)
+            j["out_b"] = torch.empty((n, S), dtype=torch.int32, device=dev)
+        jobs.append(j)
+        total += n
+    torch.cuda.synchronize()
+    stream = torch.cuda.Stream(device=dev)
+    sp = ctypes.c_void_p(stream.cuda_stream)
+
+    def P(t):
+        return ctypes.c_void_p(t.data_ptr())
+
+    def plain():
+        for j in jobs:
+            kid, n = j["key"].id, j["n"]
+            if j["op"] == ENCRYPT:
+                capi.check(lib.hg_dev_encrypt(h, kid, P(j["m"]), P(j["r"]), P(j["out_p"]), n, sp))
+            elif j["op"] == MUL:
+                capi.check(lib.hg_dev_mul(h, kid, P(j["base"]), P(j["k"]), P(j["out_p"]), n, sp))
+            elif j["op"] == ADD:
+                capi.check(lib.hg_dev_add(h, kid, P(j["base"]), P(j["other"]), P(j["out_p"]), n, sp))
+            else:
+                capi.check(lib.hg_dev_decrypt(h, kid, P(j["base"]), P(j["out_p"]), P(j["ovf"]), n, sp))
+
+    batch = hg.Batch(ctx)
+    for j in jobs:
+        if j["op"] == ENCRYPT:
+            batch.add(j["key"], ENCRYPT, j["n"], j["m"], j["r"], j["out_b"])
+        elif j["op"] == MUL:
+            batch.add(j["key"], MUL, j["n"], j["base"], j["k"], j["out_b"])
+        elif j["op"] == ADD:
+            batch.add(j["key"], ADD, j["n"], j["base"], j["other"], j["out_b"])
+        else:
+            batch.add(j["key"], DECRYPT, j["n"], j["base"], None, j["out_b"], j["ovf"])
+    # batch variant: the faster of the two layout sets on one eager run
+    best_v, best_t = 0, None
+    for v in (0, 1):
+        batch.set_variant(v)
+        batch.run(stream=stream)
+        batch.wait(stream=stream)
+        t0 = time.perf_counter()
+        batch.run(stream=stream)
+        batch.wait(stream=stream)
+        dt = time.perf_counter() - t0
+        if best_t is None or dt < best_t:
+            best_v, best_t = v, dt
+    batch.set_variant(best_v)
+
+    def timed(fn, steps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            for _ in range(steps):
+                fn()
+            e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1e3
+
+    for _ in range(args.warmup):
+        plain()
+        batch.run(stream=stream, graph=True)
+    batch.wait(stream=stream)
+    capi.check(lib.hg_dev_check(h))
+    t_plain = timed(plain, args.steps)
+    launches0 = capi.launch_count()
+    t_batch = timed(lambda: batch.run(stream=stream, graph=True), args.steps)
+    launches = capi.launch_count() - launches0
+    batch.wait(stream=stream)
+    capi.check(lib.hg_dev_check(h))
+    for j in jobs:
+        assert torch.equal(j["out_p"], j["out_b"]), "batched result differs from per-call result"
+        if j["op"] == DECRYPT:
+            assert torch.equal(j["out_b"], j["m"])
+    mix = {}
+    for j in jobs:
+        nm = {ENCRYPT: "encrypt", MUL: "mul", ADD: "add", DECRYPT: "decrypt"}[j["op"]]
+        mix[f"{nm}_{j['key'].key_bits}"] = mix.get(f"{nm}_{j['key'].key_bits}", 0) + j["n"]
+    line = {
+        "metric": "Paillier ops/s, 64 uneven jobs over 1024/2048/3072-bit keys (config 4), batched vs plain GPU",
+        "value": total * args.steps / t_batch, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_batch / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": "config4", "jobs": 64, "elements_per_step": total, "mix": mix,
+                   "batch_variant": best_v, "graph": True},
+        "plain_per_call_ops_per_s": total * args.steps / t_plain,
+        "batched_over_plain": t_plain / t_batch,
+        "gpu_launches": launches,
+    }
+    print(json.dumps(line), flush=True)
+    batch.close()
+    ctx.close()
+    return 0
+
+
+def c3_arm(args):
+    """Config 3: heu.numpy reductions with a 2048-bit key on fixed-point
+    gradients (N(0,1) * 2^20): Sum of 2^20 ciphertexts, FeatureWiseBucketSum
+    over 64 features x 256 buckets, MatMul 4096x256 ciphertexts @ 256x64
+    int32 in [-2^15, 2^15)."""
+    import numpy as np
+    import torch
+
+    import heu_gb300 as hg
+    from heu_gb300 import capi
+
+    dev = torch.device("cuda", 0)
+    ctx = hg.Context(0)
+    lib, h = ctx.lib, ctx.handle
+    key = _load_keys(ctx, [(2048, 0, 16)], not args.no_tune)[0]
+    rng = np.random.default_rng(5)
+    n, F, B = 1 << 20, 64, 256
+    M, K, N = 4096, 256, 64
+    g = torch.from_numpy(np.round(rng.standard_normal(n) * (1 << 20)).astype(np.int64)).to(dev)
+    r = torch.randint(-(2 ** 31), 2 ** 31, (n, key.r_limbs), dtype=torch.int32, device=dev)
+    ct = torch.empty((n, key.ct_limbs), dtype=torch.int32, device=dev)
+
+    def P(t):
+        return ctypes.c_void_p(t.data_ptr())
+
+    capi.check(lib.hg_dev_encrypt(h, key.id, P(g), P(r), P(ct), n, None))
+    om = torch.from_numpy(rng.integers(0, B, size=(n, F)).astype(np.uint8)).to(dev)
+    bsum = torch.empty((F * B, key.ct_limbs), dtype=torch.int32, device=dev)
+    s1 = torch.empty((1, key.ct_limbs), dtype=torch.int32, device=dev)
+    y = rng.integers(-(2 ** 15), 2 ** 15, size=(K, N), dtype=np.int64)
+    mm = torch.empty((M * N, key.ct_limbs), dtype=torch.int32, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    yc = np.ascontiguousarray(y)
+
+    def run_sum():
+        capi.check(lib.hg_dev_sum(h, key.id, P(ct), n, P(s1), sp))
+
+    def run_bucket():
+        capi.check(lib.hg_dev_bucket_sum(h, key.id, P(ct), n, 1, P(om), F, B, 0, P(bsum), sp))
+
+    def run_matmul():
+        capi.check(lib.hg_dev_matmul(h, key.id, P(ct), M, K, ctypes.c_void_p(yc.ctypes.data), N, P(mm), sp))
+
+    res = {}
+    for name, fn, units, macs_per_unit in (
+            ("sum", run_sum, n, mm_macs(128)),
+            ("bucket_sum", run_bucket, n * F, mm_macs(128)),
+            ("matmul", run_matmul, M * N, (K + 16) * mm_macs(128))):
+        for _ in range(max(1, args.warmup)):
+            fn()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            for _ in range(args.steps):
+                fn()
+            e1.record(stream)
+        torch.cuda.synchronize()
+        dt = e0.elapsed_time(e1) / 1e3 / args.steps
+        res[name] = {"seconds": dt, "units_per_s": units / dt, "algorithmic_tmacs": units * macs_per_unit / dt / 1e12}
+    capi.check(lib.hg_dev_check(h))
+    # correctness through decryption
+    key_dec = lambda t: key.decrypt(t.cpu().numpy().view(np.uint32))  # noqa: E731
+    dsum, _ = key_dec(s1)
+    assert int(dsum[0]) == int(g.sum().item())
+    db, _ = key_dec(bsum)
+    gh, omh = g.cpu().numpy(), om.cpu().numpy()
+    exact = np.zeros((F, B), dtype=np.int64)
+    for f in range(F):
+        np.add.at(exact[f], omh[:, f], gh)
+    assert np.array_equal(db.reshape(F, B), exact)
+    dm, _ = key_dec(mm)
+    assert np.array_equal(dm.reshape(M, N), gh[: M * K].reshape(M, K) @ y)
+    peak = max(capi.mac_peak(0, 0), capi.mac_peak(0, 1)) / 1e12
+    line = {
+        "metric": "heu.numpy reductions on 2048-bit ciphertexts (config 3): Sum, bucket-sum, MatMul",
+        "value": res["bucket_sum"]["units_per_s"], "unit": "ciphertext-products/s (bucket-sum)",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": "config3", "sum_n": n, "bucket_sum": [n, F, B], "matmul": [M, K, N]},
+        "results": res, "mac_peak_tmacs": peak,
+    }
+    print(json.dumps(line), flush=True)
+    ctx.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -435,12 +683,18 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", choices=["config2", "config3", "config4"], default="config2")
+    ap.add_argument("--no-tune", action="store_true", help="skip the autotuner in config3/config4")
     ap.add_argument("--ops", default="encrypt,add,mul,decrypt",
                     help="subset of the step's ops (for profiling one kernel)")
     args = ap.parse_args()
     args.ops = [o for o in args.ops.split(",") if o]
     if args.impl == "reference":
         return reference_arm(args)
+    if args.workload == "config4":
+        return c4_arm(args)
+    if args.workload == "config3":
+        return c3_arm(args)
     return ours_arm(args)
 
 

@@ -73,11 +73,34 @@ SIGNATURES = {
     "hg_dev_bucket_sum": [_P, _I, _P, _SZ, _SZ, _P, _SZ, _I, _I, _P, _P],
     "hg_matmul": [_P, _I, _P, _SZ, _SZ, _P, _SZ, _P],
     "hg_dev_matmul": [_P, _I, _P, _SZ, _SZ, _P, _SZ, _P, _P],
+    "hg_key_get_config": [_P, _I, _P],
+    "hg_key_set_config": [_P, _I, _P],
+    "hg_autotune": [_P, _I, _SZ, _P, _P],
+    "hg_batch_create": [_P, ctypes.POINTER(_P)],
+    "hg_batch_destroy": [_P],
+    "hg_batch_add": [_P, _I, _I, _SZ, _P, _P, _P, _P, _I],
+    "hg_batch_clear": [_P],
+    "hg_batch_set_variant": [_P, _I],
+    "hg_batch_run": [_P, _P, _I],
+    "hg_batch_wait": [_P, _P],
     "hg_probe_mac_peak": [_I, _I, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)],
     "hg_probe_launch_count": [ctypes.POINTER(_U64)],
 }
 
 _lib = None
+
+HG_OP_ENCRYPT, HG_OP_DECRYPT, HG_OP_ADD, HG_OP_MUL = 0, 1, 2, 3
+HG_JOB_NONNEG = 1
+
+
+class KeyConfig(ctypes.Structure):
+    """hg_key_config"""
+
+    _fields_ = [("variant", ctypes.c_int), ("dec_variant", ctypes.c_int), ("mul_window", ctypes.c_int),
+                ("dec_window", ctypes.c_int)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
 
 
 class HgError(RuntimeError):

@@ -1,0 +1,50 @@
+// Descriptors of the persistent multi-key batch kernel (batch_kernels.cu),
+// shared with the host engine.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "paillier_kernels.cuh"
+
+namespace hg {
+
+enum : int { kBatchEncrypt = 0, kBatchDecrypt = 1, kBatchAdd = 2, kBatchMul = 3 };
+
+struct BatchJob {
+  int op;      // kBatch*
+  int S;       // 32-bit limbs of n^2 (64 / 128 / 192)
+  int wm;      // scalar-mul window
+  int pad;
+  KeyConst kc;
+  SecConst sc;
+  const void* in0;  // m (int64) | ct | a | a
+  const void* in1;  // r (uint32 limbs) | - | b | k (int64)
+  void* out;        // ct | m (int64) | ct | ct
+  void* aux;        // - | overflow flags | - | -
+  uint64_t count;
+};
+
+struct BatchTile {
+  uint32_t job;
+  uint32_t start;
+  uint32_t count;
+  uint32_t pad;
+};
+
+// (threads per instance) for n^2 with S limbs and (threads per side) for p^2
+// with SP limbs, per variant; must match HG_DISPATCH_SV / HG_DISPATCH_SPV.
+__host__ __device__ constexpr int tpi_for(int S, int V) {
+  return S == 64 ? (V ? 8 : 4) : S == 128 ? (V ? 4 : 8) : (V ? 8 : 16);
+}
+__host__ __device__ constexpr int tp_for(int SP, int V) {
+  return SP == 32 ? (V ? 4 : 2) : SP == 64 ? (V ? 8 : 4) : (V ? 4 : 8);
+}
+
+int batch_resident_blocks(int variant);
+int batch_warps_per_block();
+cudaError_t launch_batch(int variant, const BatchJob* jobs, const BatchTile* tiles, uint32_t ntiles,
+                         uint32_t* counter, uint32_t* scratch, size_t warp_words, uint32_t* err, int grid,
+                         cudaStream_t st);
+
+}  // namespace hg

@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
+#include <random>
 #include <condition_variable>
 #include <cstring>
 #include <map>
@@ -15,6 +17,7 @@
 
 #include "../../include/heu_gb300.h"
 #include "../../include/heu_gb300_probe.h"
+#include "batch.cuh"
 #include "engine_internal.hpp"
 #include "host_bn.hpp"
 #include "paillier_kernels.cuh"
@@ -82,9 +85,18 @@ struct DevBuf {
   }
 };
 
+// Buffers of one product-tree inversion.
+struct TreeBufs {
+  DevBuf tree, dz;
+};
+
 struct PinBuf {
   void* p = nullptr;
   size_t n = 0;
+  template <typename T>
+  T* as() const {
+    return reinterpret_cast<T*>(p);
+  }
   ~PinBuf() {
     if (p) cudaFreeHost(p);
   }
@@ -122,6 +134,34 @@ struct KeyRec {
   int wm = 4;  // scalar-mul window
 };
 
+// Asynchronous inversion of the root of a product tree: the host function
+// runs in stream order (and as a host node inside a captured CUDA graph).
+struct InvTask {
+  const BN* N = nullptr;
+  int S = 0;
+  uint32_t* root = nullptr;  // pinned: S limbs of the root, then the kernels' error word
+  uint32_t* z = nullptr;     // pinned: S limbs of root^-1 (Z-form)
+  volatile int status = 0;   // 0 ok, 1 not invertible, 2 range error upstream
+};
+
+void CUDART_CB inv_host_fn(void* p) {
+  InvTask* t = static_cast<InvTask*>(p);
+  const size_t S = (size_t)t->S;
+  if (t->root[S] & (hg::kErrCtRange | hg::kErrPtRange)) {
+    t->status = 2;
+    for (size_t i = 0; i < S; ++i) t->z[i] = i == 0 ? 1u : 0u;
+    return;
+  }
+  try {
+    const BN z = BN::invmod(BN::from_limbs(t->root, S), *t->N);
+    z.to_limbs(t->z, S);
+    t->status = 0;
+  } catch (const std::exception&) {
+    t->status = 1;
+    for (size_t i = 0; i < S; ++i) t->z[i] = i == 0 ? 1u : 0u;
+  }
+}
+
 // Sliding-window exponent program: first window index + one op per step.
 void build_prog(const BN& e, int w, int* start, std::vector<uint16_t>* steps) {
   int i = (int)e.bitlen() - 1;
@@ -156,11 +196,13 @@ struct Work {
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   DevBuf io[6];
-  DevBuf scratch, tree, red[2], zbuf;
+  DevBuf scratch, red[2];
+  TreeBufs inv;
   DevBuf seg_cnt, seg_offs[3], seg_cursor, seg_idx, seg_nch, seg_part[2];
   DevBuf mm_tables, mm_masks, mm_prod;
   DevBuf err;
-  PinBuf pin_root, pin_err;
+  PinBuf pin_root, pin_err, pin_z;
+  InvTask task;
   ~Work() {
     if (own_stream && stream) cudaStreamDestroy(stream);
   }
@@ -253,7 +295,7 @@ void core_decrypt(KeyRec& k, Work& w, const uint32_t* ct, int64_t* m, uint8_t* o
                   size_t count) {
   if (!k.secret) fail(HG_ERR_NO_SECRET, "key has no secret part");
   const size_t ntab = (size_t)1 << (k.sc.wd - 1);
-  const size_t units = (size_t)k.grid_dec * hg::units_per_block_decrypt(k.Sp);
+  const size_t units = (size_t)k.grid_dec * hg::units_per_block_decrypt(k.Sp, k.sc.variant);
   uint32_t* scratch = w.scratch.ensure<uint32_t>(units * 2 * ntab * k.Sp * 4);
   cuda_check(hg::launch_decrypt(k.Sp, k.kc, k.sc, ct, count, m, ovf, mag, neg, scratch, w.errp(), k.grid_dec,
                                 w.stream),
@@ -261,7 +303,10 @@ void core_decrypt(KeyRec& k, Work& w, const uint32_t* ct, int64_t* m, uint8_t* o
 }
 
 // out[i] = in[i]^-1 where sel == nullptr or sel[i] < 0, else in[i].
-void core_inverse(KeyRec& k, Work& w, const uint32_t* in, const int64_t* sel, uint32_t* out, size_t count) {
+// out[i] = in[i]^-1 where sel == nullptr or sel[i] < 0, else in[i]; every
+// step is in stream order (graph-capturable).  `task` must outlive the work.
+void core_inverse_async(KeyRec& k, const uint32_t* in, const int64_t* sel, uint32_t* out, size_t count,
+                        TreeBufs& tb, InvTask& task, uint32_t* errp, cudaStream_t st) {
   if (count == 0) return;
   size_t padded = 1;
   while (padded < count) padded <<= 1;
@@ -274,43 +319,48 @@ void core_inverse(KeyRec& k, Work& w, const uint32_t* in, const int64_t* sel, ui
     total += sz;
     if (sz == 1) break;
   }
-  uint32_t* tr = w.tree.ensure<uint32_t>(total * S * 4);
-  cuda_check(hg::launch_tree_leaves(k.S, k.kc, in, sel, count, tr, padded, w.errp(), w.stream), "tree leaves");
+  uint32_t* tr = tb.tree.ensure<uint32_t>(total * S * 4);
+  uint32_t* dz = tb.dz.ensure<uint32_t>(S * 4);
+  task.N = &k.N;
+  task.S = k.S;
+  cuda_check(hg::launch_tree_leaves(k.S, k.kc, in, sel, count, tr, padded, errp, st), "tree leaves");
   for (size_t l = 0; l + 1 < off.size(); ++l) {
     const size_t up = padded >> (l + 1);
-    cuda_check(hg::launch_tree_up(k.S, k.kc, tr + off[l] * S, tr + off[l + 1] * S, up, w.stream), "tree up");
+    cuda_check(hg::launch_tree_up(k.S, k.kc, tr + off[l] * S, tr + off[l + 1] * S, up, st), "tree up");
   }
   uint32_t* root = tr + off.back() * S;
-  uint32_t* hroot = w.pin_root.ensure<uint32_t>(S * 4 + 4);
-  d2h(hroot, root, S * 4, w);
-  d2h(hroot + S, w.errp(), 4, w);
-  cuda_check(cudaStreamSynchronize(w.stream), "stream sync");
-  // a ciphertext >= n^2 among the inputs is reported before invertibility
-  raise_err_bits(hroot[S] & (hg::kErrCtRange | hg::kErrPtRange));
-  const BN x = BN::from_limbs(hroot, S);
-  BN z;
-  try {
-    z = BN::invmod(x, k.N);
-  } catch (const std::exception&) {
-    fail(HG_ERR_NOT_INVERTIBLE, "ciphertext not invertible mod n^2 (Negate/Sub/Mul with k<0)");
-  }
-  z.to_limbs(hroot, S);
-  uint32_t* dz = w.zbuf.ensure<uint32_t>(S * 4);
-  h2d(dz, hroot, S * 4, w);
-  cuda_check(hg::launch_root_fix(k.S, k.kc, dz, root, w.stream), "root fix");
+  cuda_check(cudaMemcpyAsync(task.root, root, S * 4, cudaMemcpyDeviceToHost, st), "D2H root");
+  cuda_check(cudaMemcpyAsync(task.root + S, errp, 4, cudaMemcpyDeviceToHost, st), "D2H err");
+  cuda_check(cudaLaunchHostFunc(st, inv_host_fn, &task), "host inversion");
+  cuda_check(cudaMemcpyAsync(dz, task.z, S * 4, cudaMemcpyHostToDevice, st), "H2D inverse");
+  cuda_check(hg::launch_root_fix(k.S, k.kc, dz, root, st), "root fix");
   for (size_t l = off.size() - 1; l-- > 0;) {
     const size_t up = padded >> (l + 1);
-    cuda_check(hg::launch_tree_down(k.S, k.kc, tr + off[l] * S, tr + off[l + 1] * S, up, w.stream), "tree down");
+    cuda_check(hg::launch_tree_down(k.S, k.kc, tr + off[l] * S, tr + off[l + 1] * S, up, st), "tree down");
   }
-  cuda_check(hg::launch_tree_apply(k.S, k.kc, in, sel, tr, out, count, w.stream), "tree apply");
-  // keep `hroot` valid until the copy above has been consumed
+  cuda_check(hg::launch_tree_apply(k.S, k.kc, in, sel, tr, out, count, st), "tree apply");
+}
+
+void raise_task_status(const InvTask& t) {
+  if (t.status == 2) fail(HG_ERR_CT_RANGE, "Invalid ciphertext: value >= n^2");
+  if (t.status == 1) fail(HG_ERR_NOT_INVERTIBLE, "ciphertext not invertible mod n^2 (Negate/Sub/Mul with k<0)");
+}
+
+// Synchronous form used by the host-pointer and device-pointer calls.
+void core_inverse(KeyRec& k, Work& w, const uint32_t* in, const int64_t* sel, uint32_t* out, size_t count) {
+  if (count == 0) return;
+  w.task.root = w.pin_root.ensure<uint32_t>((size_t)k.S * 4 + 4);
+  w.task.z = w.pin_z.ensure<uint32_t>((size_t)k.S * 4);
+  w.task.status = 0;
+  core_inverse_async(k, in, sel, out, count, w.inv, w.task, w.errp(), w.stream);
   cuda_check(cudaStreamSynchronize(w.stream), "stream sync");
+  raise_task_status(w.task);
 }
 
 void core_mul(KeyRec& k, Work& w, const uint32_t* a, const int64_t* kk, const int64_t* host_k, uint32_t* out,
               size_t count) {
   const size_t ntab = (size_t)1 << (k.wm - 1);
-  const size_t inst = (size_t)k.grid_mul * hg::instances_per_block(k.S);
+  const size_t inst = (size_t)k.grid_mul * hg::instances_per_block(k.S, k.kc.variant);
   uint32_t* scratch = w.scratch.ensure<uint32_t>(inst * ntab * k.S * 4);
   cuda_check(hg::launch_mul(k.S, k.kc, a, kk, out, count, scratch, k.wm, w.errp(), k.grid_mul, w.stream),
              "mul launch");
@@ -325,7 +375,7 @@ void core_mul(KeyRec& k, Work& w, const uint32_t* a, const int64_t* kk, const in
 void core_sum(KeyRec& k, Work& w, const uint32_t* a, size_t count, uint32_t* out) {
   if (count == 0) fail(HG_ERR_INVALID, "you cannot sum an empty tensor");
   const size_t S = (size_t)k.S;
-  const size_t target = (size_t)std::max(1, 152 * 4 * hg::instances_per_block(k.S));
+  const size_t target = (size_t)std::max(1, 152 * 4 * hg::instances_per_block(k.S, k.kc.variant));
   const uint32_t* cur = a;
   size_t n = count;
   int which = 0;
@@ -500,7 +550,8 @@ int load_key(hg_ctx* ctx, uint32_t key_bits, const uint32_t* n_l, const uint32_t
     for (int lv = 0; lv < kc.w; ++lv) cuda_check(hg::launch_table_level(S, kc, tab, b, lv, nullptr), "table level");
     cuda_check(cudaDeviceSynchronize(), "table build");
   }
-  k->grid_mul = hg::resident_blocks_mul(S);
+  kc.variant = 0;
+  k->grid_mul = hg::resident_blocks_mul(S, 0);
   if (p_l && q_l) {
     const int Sp = S / 2, H = S / 4;
     k->p = BN::from_limbs(p_l, H);
@@ -564,7 +615,8 @@ int load_key(hg_ctx* ctx, uint32_t key_bits, const uint32_t* n_l, const uint32_t
     }
     sc.prog[0] = dp;
     sc.prog[1] = dp + len;
-    k->grid_dec = hg::resident_blocks_decrypt(Sp);
+    sc.variant = 0;
+    k->grid_dec = hg::resident_blocks_decrypt(Sp, 0);
   }
   std::lock_guard<std::mutex> lk(ctx->mu);
   const int id = ctx->next_key++;
@@ -1111,6 +1163,443 @@ int hg_dev_matmul(hg_ctx* ctx, int key_id, const uint32_t* x, size_t M, size_t K
     return HG_OK;
   });
 }
+
+}  // extern "C"
+
+namespace {
+
+// ---- key configuration and autotuning ---------------------------------------
+static void apply_config(KeyRec& k, const hg_key_config& c) {
+  if (c.variant < 0 || c.variant > 1 || c.dec_variant < 0 || c.dec_variant > 1)
+    fail(HG_ERR_INVALID, "variant must be 0 or 1");
+  if (c.mul_window < 2 || c.mul_window > 6) fail(HG_ERR_INVALID, "mul_window must be in [2, 6]");
+  if (c.dec_window < 2 || c.dec_window > 7) fail(HG_ERR_INVALID, "dec_window must be in [2, 7]");
+  cuda_check(cudaDeviceSynchronize(), "sync");
+  k.kc.variant = c.variant;
+  k.grid_mul = hg::resident_blocks_mul(k.S, c.variant);
+  k.wm = c.mul_window;
+  if (k.secret) {
+    if (c.dec_window != k.sc.wd) {
+      std::vector<uint16_t> pp, pq;
+      int st0 = 0, st1 = 0;
+      build_prog(k.p - BN(1), c.dec_window, &st0, &pp);
+      build_prog(k.q - BN(1), c.dec_window, &st1, &pq);
+      const size_t len = std::max(pp.size(), pq.size());
+      pp.resize(len, hg::kOpNop);
+      pq.resize(len, hg::kOpNop);
+      uint16_t* dp = k.progs.ensure<uint16_t>(std::max<size_t>(2 * len, 2) * 2);
+      if (len) {
+        cuda_check(cudaMemcpy(dp, pp.data(), len * 2, cudaMemcpyHostToDevice), "upload prog");
+        cuda_check(cudaMemcpy(dp + len, pq.data(), len * 2, cudaMemcpyHostToDevice), "upload prog");
+      }
+      k.sc.prog[0] = dp;
+      k.sc.prog[1] = dp + len;
+      k.sc.prog_len = (int)len;
+      k.sc.start[0] = st0;
+      k.sc.start[1] = st1;
+      k.sc.wd = c.dec_window;
+    }
+    k.sc.variant = c.dec_variant;
+    k.grid_dec = hg::resident_blocks_decrypt(k.Sp, c.dec_variant);
+  }
+}
+
+static hg_key_config current_config(const KeyRec& k) {
+  hg_key_config c;
+  c.variant = k.kc.variant;
+  c.dec_variant = k.sc.variant;
+  c.mul_window = k.wm;
+  c.dec_window = k.secret ? k.sc.wd : 5;
+  return c;
+}
+
+// ---- persistent multi-key batches ------------------------------------------
+}  // namespace
+
+struct hg_batch {
+  struct Job {
+    int key_id, op, flags;
+    size_t count;
+    const void* in0;
+    const void* in1;
+    void* out;
+    void* aux;
+  };
+  hg_ctx* ctx = nullptr;
+  std::vector<Job> jobs;
+  bool dirty = true;
+  int variant = 0;
+  DevBuf djobs, dtiles, dcounter, derr, dscratch;
+  PinBuf pin_err;
+  uint32_t ntiles = 0;
+  size_t warp_words = 0;
+  int grid = 0;
+  struct Inv {
+    KeyRec* key;
+    size_t job;
+    TreeBufs bufs;
+    PinBuf root, z;
+    InvTask task;
+  };
+  std::vector<std::unique_ptr<Inv>> invs;
+  std::vector<KeyRec*> keys;
+  cudaGraphExec_t exec = nullptr;
+  cudaGraph_t graph = nullptr;
+  ~hg_batch() { drop_graph(); }
+  void drop_graph() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    exec = nullptr;
+    graph = nullptr;
+  }
+};
+
+namespace {
+
+// Relative cost of one ciphertext of an op (Montgomery multiplications x S^2).
+double job_cost(const KeyRec& k, int op) {
+  const double s2 = (double)k.S * k.S;
+  switch (op) {
+    case hg::kBatchEncrypt: return (k.kc.npos + 2) * s2;
+    case hg::kBatchDecrypt: return 2.0 * (k.key_bits / 2 + k.key_bits / 12) * (s2 / 4);
+    case hg::kBatchMul: return 80.0 * s2;
+    default: return s2;
+  }
+}
+
+void batch_build(hg_batch& b) {
+  const int V = b.variant;
+  std::vector<hg::BatchJob> dj;
+  struct T {
+    hg::BatchTile t;
+    double cost;
+  };
+  std::vector<T> tiles;
+  b.keys.clear();
+  b.invs.clear();
+  size_t warp_words = 1;
+  for (size_t j = 0; j < b.jobs.size(); ++j) {
+    const auto& J = b.jobs[j];
+    KeyRec* k = get_key(b.ctx, J.key_id);
+    if (J.op == hg::kBatchDecrypt && !k->secret) fail(HG_ERR_NO_SECRET, "batch decrypt job on a public key");
+    hg::BatchJob d{};
+    d.op = J.op;
+    d.S = k->S;
+    d.wm = k->wm;
+    d.kc = k->kc;
+    d.sc = k->sc;
+    d.in0 = J.in0;
+    d.in1 = J.in1;
+    d.out = J.out;
+    d.aux = J.aux;
+    d.count = J.count;
+    dj.push_back(d);
+    b.keys.push_back(k);
+    int per_pass;
+    if (J.op == hg::kBatchDecrypt) {
+      const int TP = hg::tp_for(k->Sp, V);
+      per_pass = 32 / (2 * TP);
+      warp_words = std::max(warp_words, (size_t)per_pass * 2 * ((size_t)1 << (k->sc.wd - 1)) * k->Sp);
+    } else {
+      const int TPI = hg::tpi_for(k->S, V);
+      per_pass = 32 / TPI;
+      if (J.op == hg::kBatchMul)
+        warp_words = std::max(warp_words, (size_t)per_pass * ((size_t)1 << (k->wm - 1)) * k->S);
+    }
+    const size_t tile = (size_t)per_pass * 4;
+    const double c = job_cost(*k, J.op);
+    for (size_t st = 0; st < J.count; st += tile) {
+      const size_t cnt = std::min(tile, J.count - st);
+      tiles.push_back({{(uint32_t)j, (uint32_t)st, (uint32_t)cnt, 0u}, c * (double)cnt});
+    }
+    if (J.op == hg::kBatchMul && !(J.flags & HG_JOB_NONNEG)) {
+      auto inv = std::make_unique<hg_batch::Inv>();
+      inv->key = k;
+      inv->job = j;
+      inv->task.root = inv->root.ensure<uint32_t>((size_t)k->S * 4 + 4);
+      inv->task.z = inv->z.ensure<uint32_t>((size_t)k->S * 4);
+      b.invs.push_back(std::move(inv));
+    }
+  }
+  std::stable_sort(tiles.begin(), tiles.end(), [](const T& x, const T& y) { return x.cost > y.cost; });
+  std::vector<hg::BatchTile> ht;
+  ht.reserve(tiles.size());
+  for (auto& t : tiles) ht.push_back(t.t);
+  if (tiles.size() >= (1ull << 32)) fail(HG_ERR_INVALID, "batch too large");
+  auto* jd = b.djobs.ensure<hg::BatchJob>(std::max<size_t>(dj.size(), 1) * sizeof(hg::BatchJob));
+  auto* td = b.dtiles.ensure<hg::BatchTile>(std::max<size_t>(ht.size(), 1) * sizeof(hg::BatchTile));
+  if (!dj.empty()) cuda_check(cudaMemcpy(jd, dj.data(), dj.size() * sizeof(hg::BatchJob), cudaMemcpyHostToDevice), "jobs");
+  if (!ht.empty()) cuda_check(cudaMemcpy(td, ht.data(), ht.size() * sizeof(hg::BatchTile), cudaMemcpyHostToDevice), "tiles");
+  b.ntiles = (uint32_t)ht.size();
+  b.warp_words = warp_words;
+  b.grid = hg::batch_resident_blocks(V);
+  b.dscratch.ensure<uint32_t>((size_t)b.grid * hg::batch_warps_per_block() * warp_words * 4);
+  b.dcounter.ensure<uint32_t>(4);
+  b.derr.ensure<uint32_t>(4);
+  b.pin_err.ensure<uint32_t>(4);
+  // size the inversion trees now so nothing allocates during a capture
+  for (auto& inv : b.invs) {
+    size_t padded = 1;
+    while (padded < b.jobs[inv->job].count) padded <<= 1;
+    inv->bufs.tree.ensure<uint32_t>((2 * padded) * (size_t)inv->key->S * 4);
+    inv->bufs.dz.ensure<uint32_t>((size_t)inv->key->S * 4);
+  }
+  b.dirty = false;
+}
+
+void batch_enqueue(hg_batch& b, cudaStream_t st) {
+  uint32_t* err = b.derr.as<uint32_t>();
+  cuda_check(cudaMemsetAsync(b.dcounter.p, 0, 4, st), "memset counter");
+  cuda_check(cudaMemsetAsync(err, 0, 4, st), "memset err");
+  cuda_check(hg::launch_batch(b.variant, b.djobs.as<hg::BatchJob>(), b.dtiles.as<hg::BatchTile>(), b.ntiles,
+                              b.dcounter.as<uint32_t>(), b.dscratch.as<uint32_t>(), b.warp_words, err, b.grid, st),
+             "batch launch");
+  for (auto& inv : b.invs) {
+    const auto& J = b.jobs[inv->job];
+    inv->task.status = 0;
+    core_inverse_async(*inv->key, static_cast<const uint32_t*>(J.out), static_cast<const int64_t*>(J.in1),
+                       static_cast<uint32_t*>(J.out), J.count, inv->bufs, inv->task, err, st);
+  }
+  cuda_check(cudaMemcpyAsync(b.pin_err.p, err, 4, cudaMemcpyDeviceToHost, st), "D2H err");
+}
+
+}  // namespace
+
+extern "C" {
+
+int hg_key_get_config(hg_ctx* ctx, int key_id, hg_key_config* out) {
+  return guarded([&] {
+    if (!out) fail(HG_ERR_INVALID, "null argument");
+    *out = current_config(*get_key(ctx, key_id));
+    return HG_OK;
+  });
+}
+
+int hg_key_set_config(hg_ctx* ctx, int key_id, const hg_key_config* cfg) {
+  return guarded([&] {
+    if (!cfg) fail(HG_ERR_INVALID, "null argument");
+    KeyRec* k = get_key(ctx, key_id);
+    set_device(ctx);
+    apply_config(*k, *cfg);
+    return HG_OK;
+  });
+}
+
+int hg_autotune(hg_ctx* ctx, int key_id, size_t calib, hg_key_config* best, double* rates) {
+  return guarded([&] {
+    KeyRec* k = get_key(ctx, key_id);
+    set_device(ctx);
+    const size_t n = calib ? calib : 65536;
+    LaneGuard lane(ctx);
+    Work& w = *lane.w;
+    reset_err(w);
+    std::mt19937_64 rng(12345);
+    std::vector<int64_t> m(n), kk(n);
+    std::vector<uint32_t> r(n * (size_t)k->kc.rlimbs);
+    for (auto& v : m) v = (int64_t)(rng() >> 24) - (int64_t)(1ull << 39);
+    for (auto& v : kk) v = (int64_t)(rng() >> 1);
+    for (auto& v : r) v = (uint32_t)rng();
+    const size_t cb = ct_bytes(*k);
+    auto* dm = w.io[0].ensure<int64_t>(n * 8);
+    auto* dk = w.io[1].ensure<int64_t>(n * 8);
+    auto* dr = w.io[2].ensure<uint32_t>(r.size() * 4);
+    auto* dct = w.io[3].ensure<uint32_t>(n * cb);
+    auto* dout = w.io[4].ensure<uint32_t>(n * cb);
+    auto* dm2 = w.io[5].ensure<int64_t>(n * 9);
+    h2d(dm, m.data(), n * 8, w);
+    h2d(dk, kk.data(), n * 8, w);
+    h2d(dr, r.data(), r.size() * 4, w);
+    cudaEvent_t e0, e1;
+    cuda_check(cudaEventCreate(&e0), "event");
+    cuda_check(cudaEventCreate(&e1), "event");
+    auto timed = [&](auto&& fn) {
+      fn();  // warm
+      cuda_check(cudaEventRecord(e0, w.stream), "event");
+      fn();
+      cuda_check(cudaEventRecord(e1, w.stream), "event");
+      cuda_check(cudaEventSynchronize(e1), "event sync");
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e0, e1);
+      return (double)ms * 1e-3;
+    };
+    hg_key_config c = current_config(*k), bc = c;
+    double best_nn = 1e300, t_enc = 0, t_mul = 0;
+    for (int v = 0; v < 2; ++v) {
+      c.variant = v;
+      apply_config(*k, c);
+      const double te = timed([&] { core_encrypt(*k, w, hg::EncMode::kEncrypt, dm, nullptr, nullptr, dr, nullptr, dct, n); });
+      for (int wm = 3; wm <= 5; ++wm) {
+        c.mul_window = wm;
+        apply_config(*k, c);
+        const double tm = timed([&] {
+          const size_t inst = (size_t)k->grid_mul * hg::instances_per_block(k->S, k->kc.variant);
+          uint32_t* scratch = w.scratch.ensure<uint32_t>(inst * ((size_t)1 << (k->wm - 1)) * k->S * 4);
+          cuda_check(hg::launch_mul(k->S, k->kc, dct, dk, dout, n, scratch, k->wm, w.errp(), k->grid_mul, w.stream),
+                     "mul launch");
+        });
+        if (te + tm < best_nn) {
+          best_nn = te + tm;
+          bc.variant = v;
+          bc.mul_window = wm;
+          t_enc = te;
+          t_mul = tm;
+        }
+      }
+    }
+    c.variant = bc.variant;
+    c.mul_window = bc.mul_window;
+    apply_config(*k, c);
+    double t_dec = 0;
+    if (k->secret) {
+      // fresh ciphertexts with the chosen variant
+      core_encrypt(*k, w, hg::EncMode::kEncrypt, dm, nullptr, nullptr, dr, nullptr, dct, n);
+      // enough ciphertexts for several waves of the widest layout, else the
+      // layout with more lanes per ciphertext wins on a half-empty GPU
+      const size_t wave = (size_t)hg::resident_blocks_decrypt(k->Sp, 0) * hg::units_per_block_decrypt(k->Sp, 0);
+      const size_t nd = std::min(n, std::max<size_t>(n / 2, 4 * wave));
+      double best_d = 1e300;
+      for (int dv = 0; dv < 2; ++dv)
+        for (int wd = 4; wd <= 6; ++wd) {
+          c.dec_variant = dv;
+          c.dec_window = wd;
+          apply_config(*k, c);
+          const double td = timed([&] {
+            core_decrypt(*k, w, dct, dm2, reinterpret_cast<uint8_t*>(dm2 + nd), nullptr, nullptr, nd);
+          });
+          if (td < best_d) {
+            best_d = td;
+            bc.dec_variant = dv;
+            bc.dec_window = wd;
+          }
+        }
+      t_dec = best_d / (double)nd;
+      c.dec_variant = bc.dec_variant;
+      c.dec_window = bc.dec_window;
+      apply_config(*k, c);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    finish(w);
+    if (best) *best = current_config(*k);
+    if (rates) {
+      rates[0] = (double)n / t_enc;
+      rates[1] = (double)n / t_mul;
+      rates[2] = t_dec > 0 ? 1.0 / t_dec : 0.0;
+    }
+    return HG_OK;
+  });
+}
+
+int hg_batch_create(hg_ctx* ctx, hg_batch** out) {
+  return guarded([&] {
+    if (!ctx || !out) fail(HG_ERR_INVALID, "null argument");
+    auto b = std::make_unique<hg_batch>();
+    b->ctx = ctx;
+    *out = b.release();
+    return HG_OK;
+  });
+}
+
+int hg_batch_destroy(hg_batch* b) {
+  return guarded([&] {
+    if (b) {
+      cudaSetDevice(b->ctx->device);
+      cudaDeviceSynchronize();
+      delete b;
+    }
+    return HG_OK;
+  });
+}
+
+int hg_batch_add(hg_batch* b, int key_id, int op, size_t count, const void* in0, const void* in1, void* out,
+                 void* aux, int flags) {
+  return guarded([&] {
+    if (!b) fail(HG_ERR_INVALID, "null batch");
+    if (op < hg::kBatchEncrypt || op > hg::kBatchMul) fail(HG_ERR_INVALID, "unknown batch op");
+    if (count == 0) return HG_OK;
+    if (!in0 || !out || (op != hg::kBatchDecrypt && !in1)) fail(HG_ERR_INVALID, "null job pointer");
+    if (count >= (1ull << 31)) fail(HG_ERR_INVALID, "job too large");
+    (void)get_key(b->ctx, key_id);
+    b->jobs.push_back({key_id, op, flags, count, in0, in1, out, aux});
+    b->dirty = true;
+    b->drop_graph();
+    return HG_OK;
+  });
+}
+
+int hg_batch_clear(hg_batch* b) {
+  return guarded([&] {
+    if (!b) fail(HG_ERR_INVALID, "null batch");
+    b->jobs.clear();
+    b->dirty = true;
+    b->drop_graph();
+    return HG_OK;
+  });
+}
+
+int hg_batch_set_variant(hg_batch* b, int variant) {
+  return guarded([&] {
+    if (!b || variant < 0 || variant > 1) fail(HG_ERR_INVALID, "variant must be 0 or 1");
+    if (variant != b->variant) {
+      b->variant = variant;
+      b->dirty = true;
+      b->drop_graph();
+    }
+    return HG_OK;
+  });
+}
+
+int hg_batch_run(hg_batch* b, void* stream, int use_graph) {
+  return guarded([&] {
+    if (!b) fail(HG_ERR_INVALID, "null batch");
+    set_device(b->ctx);
+    cudaStream_t st = stream ? (cudaStream_t)stream : b->ctx->lanes[0]->stream;
+    if (b->dirty) batch_build(*b);
+    if (!use_graph) {
+      batch_enqueue(*b, st);
+      return HG_OK;
+    }
+    if (!b->exec) {
+      // every buffer is sized by batch_build; capture the whole sequence once
+      cuda_check(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");
+      try {
+        batch_enqueue(*b, st);
+      } catch (...) {
+        cudaGraph_t g = nullptr;
+        cudaStreamEndCapture(st, &g);
+        if (g) cudaGraphDestroy(g);
+        throw;
+      }
+      cuda_check(cudaStreamEndCapture(st, &b->graph), "end capture");
+      cuda_check(cudaGraphInstantiate(&b->exec, b->graph, 0), "graph instantiate");
+    }
+    cuda_check(cudaGraphLaunch(b->exec, st), "graph launch");
+    uint64_t per_run = 1;
+    for (auto& inv : b->invs) {
+      size_t padded = 1, levels = 0;
+      while (padded < b->jobs[inv->job].count) {
+        padded <<= 1;
+        ++levels;
+      }
+      per_run += 2 * levels + 3;
+    }
+    hg::count_launches(per_run);
+    return HG_OK;
+  });
+}
+
+int hg_batch_wait(hg_batch* b, void* stream) {
+  return guarded([&] {
+    if (!b) fail(HG_ERR_INVALID, "null batch");
+    set_device(b->ctx);
+    cudaStream_t st = stream ? (cudaStream_t)stream : b->ctx->lanes[0]->stream;
+    cuda_check(cudaStreamSynchronize(st), "stream sync");
+    raise_err_bits(*b->pin_err.as<uint32_t>());
+    for (auto& inv : b->invs) raise_task_status(inv->task);
+    return HG_OK;
+  });
+}
+
 
 int hg_probe_launch_count(uint64_t* out) {
   if (!out) return HG_ERR_INVALID;

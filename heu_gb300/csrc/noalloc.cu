@@ -107,7 +107,7 @@ extern "C" int hg_dev_sum_noalloc(hg_ctx* ctx, int key_id, const uint32_t* a, si
     size_t n = count;
     int which = 0;
     bool first = true;
-    const size_t target = (size_t)std::max(1, 152 * 4 * hg::instances_per_block(S));
+    const size_t target = (size_t)std::max(1, 152 * 4 * hg::instances_per_block(S, kc.variant));
     while (n > 1 && ce == cudaSuccess) {
       size_t chunk;
       if (first) {

@@ -31,6 +31,7 @@ struct KeyConst {
   int npos;             // digit positions = ceil(rbits / w)
   int rbits;            // bits of the encryption randomness r (k/2)
   int rlimbs;           // 32-bit limbs per r
+  int variant;          // (threads per instance, limbs per thread) variant, 0 or 1
 };
 
 // Secret-key constants for CRT decryption.  Index 0 = p side, 1 = q side.
@@ -47,6 +48,7 @@ struct SecConst {
   int prog_len;             // both programs padded to this many steps
   int wd;                   // decryption window bits
   int Sp;                   // 32-bit limbs of p^2
+  int variant;              // (threads per unit side, limbs per thread) variant
 };
 
 // Exponent-program opcodes (one Montgomery multiplication per step).
@@ -114,13 +116,13 @@ cudaError_t launch_scale_rows(int S, const KeyConst& kc, uint32_t* out, const ui
 size_t subset_table_bytes_per_row(int S, int K);
 
 // Occupancy-derived grid sizes (blocks) for the persistent kernels.
-int resident_blocks_encrypt(int S);
-int resident_blocks_mul(int S);
-int resident_blocks_decrypt(int Sp);
-int instances_per_block(int S);
-int units_per_block_decrypt(int Sp);
+int resident_blocks_mul(int S, int variant);
+int resident_blocks_decrypt(int Sp, int variant);
+int instances_per_block(int S, int variant);
+int units_per_block_decrypt(int Sp, int variant);
 
 bool supported_limbs(int S);
 uint64_t launch_count();  // kernels launched by this process so far
+void count_launches(uint64_t n);
 
 }  // namespace hg

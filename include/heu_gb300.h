@@ -133,6 +133,52 @@ int hg_matmul(hg_ctx* ctx, int key_id, const uint32_t* x, size_t M, size_t K, co
 int hg_to_mont(hg_ctx* ctx, int key_id, const uint32_t* z, uint32_t* mont, size_t count);
 int hg_from_mont(hg_ctx* ctx, int key_id, const uint32_t* mont, uint32_t* z, size_t count);
 
+/* ---- per-key tuning (no counterpart in the reference) --------------------
+ * (threads per ciphertext, limbs per thread) variant and window widths.  The
+ * results do not depend on the configuration, only the speed does.        */
+typedef struct {
+  int variant;     /* mod n^2 ops: 0 = default layout, 1 = alternative */
+  int dec_variant; /* mod p^2 (CRT decryption): 0 or 1 */
+  int mul_window;  /* sliding-window bits of scalar Mul, 2..6 */
+  int dec_window;  /* sliding-window bits of CRT decryption, 2..7 */
+} hg_key_config;
+int hg_key_get_config(hg_ctx* ctx, int key_id, hg_key_config* out);
+int hg_key_set_config(hg_ctx* ctx, int key_id, const hg_key_config* cfg);
+/* Project autotuner: times encrypt and mul (both variants, mul windows 3..5)
+ * and decrypt (both variants, windows 4..6) on `calib` random inputs
+ * (0 = 65536; decryption uses enough of them for several full waves),
+ * applies the fastest configuration and returns it; rates[0..2] receive
+ * encrypt, mul and decrypt ops/s at that configuration.  Calibrate with at
+ * least as many inputs as a production call fills the GPU with.          */
+int hg_autotune(hg_ctx* ctx, int key_id, size_t calib, hg_key_config* best, double* rates);
+
+/* ---- persistent multi-key batches (no counterpart in the reference) -----
+ * A batch holds jobs of any loaded keys (1024/2048/3072 bits) and ops, all on
+ * DEVICE pointers: ENCRYPT (in0 = int64 m, in1 = r limbs, out = ct),
+ * DECRYPT (in0 = ct, out = int64 m, aux = overflow flags), ADD (in0, in1 =
+ * ct, out = ct), MUL (in0 = ct, in1 = int64 k, out = ct; HG_JOB_NONNEG
+ * promises k >= 0 and skips the inverse pass).  hg_batch_run executes every
+ * job in ONE persistent kernel launch (warps take cost-ordered tiles from a
+ * device queue), followed by the batch inverses of negative scalars; with
+ * use_graph the whole sequence is captured once into a CUDA graph and
+ * replayed on later runs (the host inversion becomes a host node).  Runs are
+ * asynchronous on `stream`; hg_batch_wait synchronises and reports errors.
+ * A batch keeps copies of its keys' constants: free no key it uses.      */
+typedef struct hg_batch hg_batch;
+#define HG_OP_ENCRYPT 0
+#define HG_OP_DECRYPT 1
+#define HG_OP_ADD 2
+#define HG_OP_MUL 3
+#define HG_JOB_NONNEG 1
+int hg_batch_create(hg_ctx* ctx, hg_batch** out);
+int hg_batch_destroy(hg_batch* b);
+int hg_batch_add(hg_batch* b, int key_id, int op, size_t count, const void* in0, const void* in1, void* out,
+                 void* aux, int flags);
+int hg_batch_clear(hg_batch* b);
+int hg_batch_set_variant(hg_batch* b, int variant);
+int hg_batch_run(hg_batch* b, void* stream, int use_graph);
+int hg_batch_wait(hg_batch* b, void* stream);
+
 /* ---- device-pointer forms (asynchronous on `stream`) --------------------
  * Same semantics as the host forms above.  Range errors raised by kernels
  * are collected per context; hg_dev_check(ctx) synchronises and reports
