@@ -672,6 +672,146 @@ def c3_arm(args):
     return 0
 
 
+def c5_arm(args):
+    """Config 5: served request stream.  8 resident keypairs (six 2048-bit,
+    two 3072-bit), Poisson arrivals at swept rates, lengths log-uniform in
+    [1, 65536], op mix encrypt/add/mul/sum/decrypt 30/20/25/15/10, resident
+    ciphertext vectors, 40 GB device budget; p50/p99 latency and throughput
+    per rate, against the same mix through plain per-call kernels."""
+    import numpy as np
+    import torch
+
+    import heu_gb300 as hg
+    from heu_gb300 import autotune, capi
+
+    dev = torch.device("cuda", 0)
+    ctx = hg.Context(0)
+    lib, h = ctx.lib, ctx.handle
+    spec = [(2048, s, 16) for s in range(6)] + [(3072, 10 + s, 14) for s in range(2)]
+    keys = _load_keys(ctx, spec, False)
+    if not args.no_tune:
+        c2048, _ = autotune.tune(keys[0], calib=131072)
+        c3072, _ = autotune.tune(keys[6], calib=65536)
+        for kk in keys[1:6]:
+            autotune.set_config(kk, c2048)
+        autotune.set_config(keys[7], c3072)
+    LMAX = 65536
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(55)
+    dev_vecs, handles = [], []
+
+    def P(t):
+        return ctypes.c_void_p(t.data_ptr())
+
+    server = hg.Server(ctx, budget_bytes=40 << 30, slots=4, max_batch_elems=1 << 18)
+    for key in keys:
+        m = torch.randint(-(2 ** 40), 2 ** 40, (LMAX,), dtype=torch.int64, device=dev, generator=gen)
+        r = torch.randint(-(2 ** 31), 2 ** 31, (LMAX, key.r_limbs), dtype=torch.int32, device=dev, generator=gen)
+        ct = torch.empty((LMAX, key.ct_limbs), dtype=torch.int32, device=dev)
+        capi.check(lib.hg_dev_encrypt(h, key.id, P(m), P(r), P(ct), LMAX, None))
+        torch.cuda.synchronize()
+        dev_vecs.append(ct)
+        handles.append(server.store(key, ct.cpu().numpy().view(np.uint32)))
+    maxS, maxRL = 192, 48
+    m_host = torch.randint(-(2 ** 62), 2 ** 62, (LMAX,), dtype=torch.int64).pin_memory()
+    r_host = torch.randint(-(2 ** 31), 2 ** 31, (LMAX, maxRL), dtype=torch.int32).pin_memory()
+    k_host = torch.randint(-(2 ** 63), 2 ** 63 - 1, (LMAX,), dtype=torch.int64).pin_memory()
+    sink = torch.empty((LMAX, maxS), dtype=torch.int32).pin_memory()
+    key_ids = (ctypes.c_int * len(keys))(*[k.id for k in keys])
+    hnd = (ctypes.c_uint64 * len(keys))(*handles)
+    weights = [0.30, 0.20, 0.25, 0.15, 0.10]  # encrypt, add, mul, sum, decrypt
+    rates = [100, 300, 1000, 3000, 10000, 50000] if not args.quick else [300, 3000]
+    results = []
+    # warm-up: a short stream
+    for rate, nreq, seed in [(1000, 50, 1)] + [(rt, 0, 0) for rt in rates]:
+        if nreq == 0:
+            nreq = min(1000, max(200, int(rate * 3)))
+            seed = int(rate)
+        ls = capi.LoadSpec()
+        ls.key_ids = ctypes.cast(key_ids, ctypes.c_void_p)
+        ls.nkeys = len(keys)
+        ls.handles = ctypes.cast(hnd, ctypes.c_void_p)
+        ls.rate = float(rate)
+        ls.nreq = nreq
+        ls.len_min, ls.len_max = 1, LMAX
+        for i, wv in enumerate(weights):
+            ls.op_weights[i] = wv
+        ls.seed = seed
+        ls.m_host, ls.r_host, ls.k_host, ls.sink = (m_host.data_ptr(), r_host.data_ptr(), k_host.data_ptr(),
+                                                    sink.data_ptr())
+        lat = np.zeros(nreq, dtype=np.float64)
+        ops = np.zeros(nreq, dtype=np.int32)
+        lens = np.zeros(nreq, dtype=np.uint64)
+        wall = ctypes.c_double()
+        b0 = server.stats()["batches"]
+        capi.check(lib.hg_probe_serve_load(server.handle, ctypes.byref(ls), ctypes.c_void_p(lat.ctypes.data),
+                                           ctypes.c_void_p(ops.ctypes.data), ctypes.c_void_p(lens.ctypes.data),
+                                           ctypes.byref(wall)))
+        if seed == 1:
+            continue
+        nb = server.stats()["batches"] - b0
+        results.append({"rate_req_per_s": rate, "requests": nreq,
+                        "p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
+                        "mean_ms": float(lat.mean() * 1e3),
+                        "throughput_req_per_s": nreq / wall.value,
+                        "throughput_ops_per_s": float(lens.sum()) / wall.value,
+                        "micro_batches": int(nb), "wall_s": wall.value})
+    # the same mix through plain per-call kernels (device-resident inputs, one stream)
+    rng = np.random.default_rng(99)
+    mix = []
+    for _ in range(300):
+        ki = int(rng.integers(len(keys)))
+        n = int(min(LMAX, max(1, np.floor(np.exp(rng.uniform(0, np.log(LMAX + 1)))))))
+        mix.append((ki, int(rng.choice(5, p=weights)), n))
+    m_d = m_host.to(dev)
+    r_d = r_host.to(dev)
+    k_d = k_host.to(dev)
+    out_ct = torch.empty((LMAX, maxS), dtype=torch.int32, device=dev)
+    out_m = torch.empty((LMAX,), dtype=torch.int64, device=dev)
+    ovf = torch.empty((LMAX,), dtype=torch.uint8, device=dev)
+    st = torch.cuda.Stream(device=dev)
+    sp = ctypes.c_void_p(st.cuda_stream)
+
+    def plain():
+        for ki, op, n in mix:
+            key, vec = keys[ki], dev_vecs[ki]
+            if op == 0:
+                capi.check(lib.hg_dev_encrypt(h, key.id, P(m_d), P(r_d), P(out_ct), n, sp))
+            elif op == 1:
+                capi.check(lib.hg_dev_add(h, key.id, P(vec), P(vec), P(out_ct), n, sp))
+            elif op == 2:
+                capi.check(lib.hg_dev_mul(h, key.id, P(vec), P(k_d), P(out_ct), n, sp))
+            elif op == 3:
+                capi.check(lib.hg_dev_sum(h, key.id, P(vec), n, P(out_ct), sp))
+            else:
+                capi.check(lib.hg_dev_decrypt(h, key.id, P(vec), P(out_m), P(ovf), n, sp))
+
+    plain()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    plain()
+    torch.cuda.synchronize()
+    t_plain = time.perf_counter() - t0
+    capi.check(lib.hg_dev_check(h))
+    plain_ops = sum(n for _, _, n in mix) / t_plain
+    peak_served = max(r["throughput_ops_per_s"] for r in results)
+    line = {
+        "metric": "Served Paillier request stream (config 5): p50/p99 latency and throughput",
+        "value": peak_served, "unit": "ops/s", "n_gpus": 1, "steps": len(results), "warmup": 1,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": "config5", "keys": "6x2048 + 2x3072 resident", "len": [1, LMAX],
+                   "op_mix": dict(zip(["encrypt", "add", "mul", "sum", "decrypt"], weights)),
+                   "budget_bytes": 40 << 30, "slots": 4, "max_batch_elems": 1 << 18},
+        "rates": results,
+        "plain_per_call_ops_per_s": plain_ops,
+        "served_over_plain": peak_served / plain_ops,
+    }
+    print(json.dumps(line), flush=True)
+    server.close()
+    ctx.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -683,8 +823,9 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", choices=["config2", "config3", "config4"], default="config2")
-    ap.add_argument("--no-tune", action="store_true", help="skip the autotuner in config3/config4")
+    ap.add_argument("--workload", choices=["config2", "config3", "config4", "config5"], default="config2")
+    ap.add_argument("--no-tune", action="store_true", help="skip the autotuner")
+    ap.add_argument("--quick", action="store_true", help="config5: two arrival rates only")
     ap.add_argument("--ops", default="encrypt,add,mul,decrypt",
                     help="subset of the step's ops (for profiling one kernel)")
     args = ap.parse_args()
@@ -695,6 +836,8 @@ def main():
         return c4_arm(args)
     if args.workload == "config3":
         return c3_arm(args)
+    if args.workload == "config5":
+        return c5_arm(args)
     return ours_arm(args)
 
 

@@ -8,3 +8,4 @@ CPU fallback.
 from heu_gb300.capi import HgError, load  # noqa: F401
 from heu_gb300.engine import Context, Key, ints_to_limbs, keygen, limbs_to_ints  # noqa: F401
 from heu_gb300.batch import Batch  # noqa: F401,E402
+from heu_gb300.server import Server  # noqa: F401,E402

@@ -83,14 +83,47 @@ SIGNATURES = {
     "hg_batch_set_variant": [_P, _I],
     "hg_batch_run": [_P, _P, _I],
     "hg_batch_wait": [_P, _P],
+    "hg_server_create": [_P, _P, ctypes.POINTER(_P)],
+    "hg_server_destroy": [_P],
+    "hg_server_store": [_P, _I, _P, _SZ, ctypes.POINTER(_U64)],
+    "hg_server_release": [_P, _U64],
+    "hg_server_submit": [_P, _P, ctypes.POINTER(_U64)],
+    "hg_server_wait": [_P, _U64, ctypes.POINTER(ctypes.c_double)],
+    "hg_server_stats": [_P, ctypes.POINTER(_U64), ctypes.POINTER(_U64), ctypes.POINTER(_SZ), ctypes.POINTER(_SZ)],
+    "hg_probe_serve_load": [_P, _P, _P, _P, _P, ctypes.POINTER(ctypes.c_double)],
     "hg_probe_mac_peak": [_I, _I, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)],
     "hg_probe_launch_count": [ctypes.POINTER(_U64)],
 }
 
 _lib = None
 
-HG_OP_ENCRYPT, HG_OP_DECRYPT, HG_OP_ADD, HG_OP_MUL = 0, 1, 2, 3
+HG_OP_ENCRYPT, HG_OP_DECRYPT, HG_OP_ADD, HG_OP_MUL, HG_OP_SUM = 0, 1, 2, 3, 4
 HG_JOB_NONNEG = 1
+
+
+class ServerConfig(ctypes.Structure):
+    """hg_server_config"""
+
+    _fields_ = [("budget_bytes", ctypes.c_size_t), ("slots", ctypes.c_int), ("max_batch_elems", ctypes.c_size_t),
+                ("variant", ctypes.c_int), ("batch_us", ctypes.c_double), ("slice_us", ctypes.c_double)]
+
+
+class Request(ctypes.Structure):
+    """hg_request"""
+
+    _fields_ = [("key_id", ctypes.c_int), ("op", ctypes.c_int), ("count", ctypes.c_size_t),
+                ("in0", ctypes.c_void_p), ("in1", ctypes.c_void_p), ("h0", ctypes.c_uint64),
+                ("h1", ctypes.c_uint64), ("out", ctypes.c_void_p), ("aux", ctypes.c_void_p)]
+
+
+class LoadSpec(ctypes.Structure):
+    """hg_load_spec"""
+
+    _fields_ = [("key_ids", ctypes.c_void_p), ("nkeys", ctypes.c_int), ("handles", ctypes.c_void_p),
+                ("rate", ctypes.c_double), ("nreq", ctypes.c_size_t), ("len_min", ctypes.c_size_t),
+                ("len_max", ctypes.c_size_t), ("op_weights", ctypes.c_double * 5), ("seed", ctypes.c_uint64),
+                ("m_host", ctypes.c_void_p), ("r_host", ctypes.c_void_p), ("k_host", ctypes.c_void_p),
+                ("sink", ctypes.c_void_p)]
 
 
 class KeyConfig(ctypes.Structure):

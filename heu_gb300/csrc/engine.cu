@@ -7,6 +7,9 @@
 #include <chrono>
 #include <random>
 #include <condition_variable>
+#include <deque>
+#include <thread>
+#include <unordered_map>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -87,7 +90,7 @@ struct DevBuf {
 
 // Buffers of one product-tree inversion.
 struct TreeBufs {
-  DevBuf tree, dz;
+  DevBuf tree;
 };
 
 struct PinBuf {
@@ -140,7 +143,7 @@ struct InvTask {
   const BN* N = nullptr;
   int S = 0;
   uint32_t* root = nullptr;  // pinned: S limbs of the root, then the kernels' error word
-  uint32_t* z = nullptr;     // pinned: S limbs of root^-1 (Z-form)
+  uint32_t* z = nullptr;     // pinned: S limbs of the root's inverse, Montgomery form
   volatile int status = 0;   // 0 ok, 1 not invertible, 2 range error upstream
 };
 
@@ -149,16 +152,15 @@ void CUDART_CB inv_host_fn(void* p) {
   const size_t S = (size_t)t->S;
   if (t->root[S] & (hg::kErrCtRange | hg::kErrPtRange)) {
     t->status = 2;
-    for (size_t i = 0; i < S; ++i) t->z[i] = i == 0 ? 1u : 0u;
+    for (size_t i = 0; i < S; ++i) t->z[i] = 0u;
     return;
   }
-  try {
-    const BN z = BN::invmod(BN::from_limbs(t->root, S), *t->N);
-    z.to_limbs(t->z, S);
+  // root = X*R; the tree's down-sweep wants X^-1 * R
+  if (hg::mont_root_inverse(t->root, *t->N, S, t->z)) {
     t->status = 0;
-  } catch (const std::exception&) {
+  } else {
     t->status = 1;
-    for (size_t i = 0; i < S; ++i) t->z[i] = i == 0 ? 1u : 0u;
+    for (size_t i = 0; i < S; ++i) t->z[i] = 0u;
   }
 }
 
@@ -305,8 +307,22 @@ void core_decrypt(KeyRec& k, Work& w, const uint32_t* ct, int64_t* m, uint8_t* o
 // out[i] = in[i]^-1 where sel == nullptr or sel[i] < 0, else in[i].
 // out[i] = in[i]^-1 where sel == nullptr or sel[i] < 0, else in[i]; every
 // step is in stream order (graph-capturable).  `task` must outlive the work.
+void core_inverse_async_raw(KeyRec& k, const uint32_t* in, const int64_t* sel, uint32_t* out, size_t count,
+                            uint32_t* tr, InvTask& task, uint32_t* errp, cudaStream_t st);
+
 void core_inverse_async(KeyRec& k, const uint32_t* in, const int64_t* sel, uint32_t* out, size_t count,
                         TreeBufs& tb, InvTask& task, uint32_t* errp, cudaStream_t st) {
+  if (count == 0) return;
+  size_t padded = 1;
+  while (padded < count) padded <<= 1;
+  const size_t S = (size_t)k.S;
+  uint32_t* tr = tb.tree.ensure<uint32_t>(2 * padded * S * 4);
+  core_inverse_async_raw(k, in, sel, out, count, tr, task, errp, st);
+}
+
+// Same, on a caller-provided tree buffer of 2 * padded ciphertexts.
+void core_inverse_async_raw(KeyRec& k, const uint32_t* in, const int64_t* sel, uint32_t* out, size_t count,
+                            uint32_t* tr, InvTask& task, uint32_t* errp, cudaStream_t st) {
   if (count == 0) return;
   size_t padded = 1;
   while (padded < count) padded <<= 1;
@@ -319,8 +335,6 @@ void core_inverse_async(KeyRec& k, const uint32_t* in, const int64_t* sel, uint3
     total += sz;
     if (sz == 1) break;
   }
-  uint32_t* tr = tb.tree.ensure<uint32_t>(total * S * 4);
-  uint32_t* dz = tb.dz.ensure<uint32_t>(S * 4);
   task.N = &k.N;
   task.S = k.S;
   cuda_check(hg::launch_tree_leaves(k.S, k.kc, in, sel, count, tr, padded, errp, st), "tree leaves");
@@ -332,8 +346,7 @@ void core_inverse_async(KeyRec& k, const uint32_t* in, const int64_t* sel, uint3
   cuda_check(cudaMemcpyAsync(task.root, root, S * 4, cudaMemcpyDeviceToHost, st), "D2H root");
   cuda_check(cudaMemcpyAsync(task.root + S, errp, 4, cudaMemcpyDeviceToHost, st), "D2H err");
   cuda_check(cudaLaunchHostFunc(st, inv_host_fn, &task), "host inversion");
-  cuda_check(cudaMemcpyAsync(dz, task.z, S * 4, cudaMemcpyHostToDevice, st), "H2D inverse");
-  cuda_check(hg::launch_root_fix(k.S, k.kc, dz, root, st), "root fix");
+  cuda_check(cudaMemcpyAsync(root, task.z, S * 4, cudaMemcpyHostToDevice, st), "H2D inverse");
   for (size_t l = off.size() - 1; l-- > 0;) {
     const size_t up = padded >> (l + 1);
     cuda_check(hg::launch_tree_down(k.S, k.kc, tr + off[l] * S, tr + off[l + 1] * S, up, st), "tree down");
@@ -1267,20 +1280,34 @@ double job_cost(const KeyRec& k, int op) {
   }
 }
 
-void batch_build(hg_batch& b) {
-  const int V = b.variant;
-  std::vector<hg::BatchJob> dj;
+// One job of a persistent batch, resolved against its key.
+struct JobSpec {
+  KeyRec* k;
+  int op, flags;
+  size_t count;
+  const void* in0;
+  const void* in1;
+  void* out;
+  void* aux;
+};
+
+// Host-side plan of a batch: descriptors, cost-ordered tiles, scratch size.
+struct BatchPlan {
+  std::vector<hg::BatchJob> jobs;
+  std::vector<hg::BatchTile> tiles;
+  size_t warp_words = 1;
+};
+
+BatchPlan plan_batch(const std::vector<JobSpec>& specs, int V) {
+  BatchPlan plan;
   struct T {
     hg::BatchTile t;
     double cost;
   };
   std::vector<T> tiles;
-  b.keys.clear();
-  b.invs.clear();
-  size_t warp_words = 1;
-  for (size_t j = 0; j < b.jobs.size(); ++j) {
-    const auto& J = b.jobs[j];
-    KeyRec* k = get_key(b.ctx, J.key_id);
+  for (size_t j = 0; j < specs.size(); ++j) {
+    const JobSpec& J = specs[j];
+    KeyRec* k = J.k;
     if (J.op == hg::kBatchDecrypt && !k->secret) fail(HG_ERR_NO_SECRET, "batch decrypt job on a public key");
     hg::BatchJob d{};
     d.op = J.op;
@@ -1293,18 +1320,17 @@ void batch_build(hg_batch& b) {
     d.out = J.out;
     d.aux = J.aux;
     d.count = J.count;
-    dj.push_back(d);
-    b.keys.push_back(k);
+    plan.jobs.push_back(d);
     int per_pass;
     if (J.op == hg::kBatchDecrypt) {
       const int TP = hg::tp_for(k->Sp, V);
       per_pass = 32 / (2 * TP);
-      warp_words = std::max(warp_words, (size_t)per_pass * 2 * ((size_t)1 << (k->sc.wd - 1)) * k->Sp);
+      plan.warp_words = std::max(plan.warp_words, (size_t)per_pass * 2 * ((size_t)1 << (k->sc.wd - 1)) * k->Sp);
     } else {
       const int TPI = hg::tpi_for(k->S, V);
       per_pass = 32 / TPI;
       if (J.op == hg::kBatchMul)
-        warp_words = std::max(warp_words, (size_t)per_pass * ((size_t)1 << (k->wm - 1)) * k->S);
+        plan.warp_words = std::max(plan.warp_words, (size_t)per_pass * ((size_t)1 << (k->wm - 1)) * k->S);
     }
     const size_t tile = (size_t)per_pass * 4;
     const double c = job_cost(*k, J.op);
@@ -1312,6 +1338,30 @@ void batch_build(hg_batch& b) {
       const size_t cnt = std::min(tile, J.count - st);
       tiles.push_back({{(uint32_t)j, (uint32_t)st, (uint32_t)cnt, 0u}, c * (double)cnt});
     }
+  }
+  if (tiles.size() >= (1ull << 32)) fail(HG_ERR_INVALID, "batch too large");
+  std::stable_sort(tiles.begin(), tiles.end(), [](const T& x, const T& y) { return x.cost > y.cost; });
+  plan.tiles.reserve(tiles.size());
+  for (auto& t : tiles) plan.tiles.push_back(t.t);
+  return plan;
+}
+
+size_t padded_pow2(size_t n) {
+  size_t p = 1;
+  while (p < n) p <<= 1;
+  return p;
+}
+
+void batch_build(hg_batch& b) {
+  const int V = b.variant;
+  std::vector<JobSpec> specs;
+  b.keys.clear();
+  b.invs.clear();
+  for (size_t j = 0; j < b.jobs.size(); ++j) {
+    const auto& J = b.jobs[j];
+    KeyRec* k = get_key(b.ctx, J.key_id);
+    specs.push_back({k, J.op, J.flags, J.count, J.in0, J.in1, J.out, J.aux});
+    b.keys.push_back(k);
     if (J.op == hg::kBatchMul && !(J.flags & HG_JOB_NONNEG)) {
       auto inv = std::make_unique<hg_batch::Inv>();
       inv->key = k;
@@ -1321,28 +1371,26 @@ void batch_build(hg_batch& b) {
       b.invs.push_back(std::move(inv));
     }
   }
-  std::stable_sort(tiles.begin(), tiles.end(), [](const T& x, const T& y) { return x.cost > y.cost; });
-  std::vector<hg::BatchTile> ht;
-  ht.reserve(tiles.size());
-  for (auto& t : tiles) ht.push_back(t.t);
-  if (tiles.size() >= (1ull << 32)) fail(HG_ERR_INVALID, "batch too large");
-  auto* jd = b.djobs.ensure<hg::BatchJob>(std::max<size_t>(dj.size(), 1) * sizeof(hg::BatchJob));
-  auto* td = b.dtiles.ensure<hg::BatchTile>(std::max<size_t>(ht.size(), 1) * sizeof(hg::BatchTile));
-  if (!dj.empty()) cuda_check(cudaMemcpy(jd, dj.data(), dj.size() * sizeof(hg::BatchJob), cudaMemcpyHostToDevice), "jobs");
-  if (!ht.empty()) cuda_check(cudaMemcpy(td, ht.data(), ht.size() * sizeof(hg::BatchTile), cudaMemcpyHostToDevice), "tiles");
-  b.ntiles = (uint32_t)ht.size();
-  b.warp_words = warp_words;
+  const BatchPlan plan = plan_batch(specs, V);
+  auto* jd = b.djobs.ensure<hg::BatchJob>(std::max<size_t>(plan.jobs.size(), 1) * sizeof(hg::BatchJob));
+  auto* td = b.dtiles.ensure<hg::BatchTile>(std::max<size_t>(plan.tiles.size(), 1) * sizeof(hg::BatchTile));
+  if (!plan.jobs.empty())
+    cuda_check(cudaMemcpy(jd, plan.jobs.data(), plan.jobs.size() * sizeof(hg::BatchJob), cudaMemcpyHostToDevice),
+               "jobs");
+  if (!plan.tiles.empty())
+    cuda_check(cudaMemcpy(td, plan.tiles.data(), plan.tiles.size() * sizeof(hg::BatchTile), cudaMemcpyHostToDevice),
+               "tiles");
+  b.ntiles = (uint32_t)plan.tiles.size();
+  b.warp_words = plan.warp_words;
   b.grid = hg::batch_resident_blocks(V);
-  b.dscratch.ensure<uint32_t>((size_t)b.grid * hg::batch_warps_per_block() * warp_words * 4);
+  b.dscratch.ensure<uint32_t>((size_t)b.grid * hg::batch_warps_per_block() * plan.warp_words * 4);
   b.dcounter.ensure<uint32_t>(4);
   b.derr.ensure<uint32_t>(4);
   b.pin_err.ensure<uint32_t>(4);
   // size the inversion trees now so nothing allocates during a capture
   for (auto& inv : b.invs) {
-    size_t padded = 1;
-    while (padded < b.jobs[inv->job].count) padded <<= 1;
+    const size_t padded = padded_pow2(b.jobs[inv->job].count);
     inv->bufs.tree.ensure<uint32_t>((2 * padded) * (size_t)inv->key->S * 4);
-    inv->bufs.dz.ensure<uint32_t>((size_t)inv->key->S * 4);
   }
   b.dirty = false;
 }
@@ -1364,6 +1412,8 @@ void batch_enqueue(hg_batch& b, cudaStream_t st) {
 }
 
 }  // namespace
+
+#include "server_impl.hpp"
 
 extern "C" {
 
@@ -1581,7 +1631,7 @@ int hg_batch_run(hg_batch* b, void* stream, int use_graph) {
         padded <<= 1;
         ++levels;
       }
-      per_run += 2 * levels + 3;
+      per_run += 2 * levels + 2;
     }
     hg::count_launches(per_run);
     return HG_OK;
@@ -1600,6 +1650,227 @@ int hg_batch_wait(hg_batch* b, void* stream) {
   });
 }
 
+
+
+int hg_server_create(hg_ctx* ctx, const hg_server_config* cfg, hg_server** out) {
+  return guarded([&] {
+    if (!ctx || !out) fail(HG_ERR_INVALID, "null argument");
+    set_device(ctx);
+    auto s = std::make_unique<hg_server>();
+    s->ctx = ctx;
+    hg_server_config c{};
+    c.budget_bytes = (size_t)40 << 30;
+    c.slots = 4;
+    c.max_batch_elems = 1 << 20;
+    c.variant = 0;
+    if (cfg) {
+      if (cfg->budget_bytes) c.budget_bytes = cfg->budget_bytes;
+      if (cfg->slots > 0) c.slots = cfg->slots;
+      if (cfg->max_batch_elems) c.max_batch_elems = cfg->max_batch_elems;
+      c.variant = cfg->variant;
+    }
+    if (c.variant < 0 || c.variant > 1) fail(HG_ERR_INVALID, "variant must be 0 or 1");
+    s->cfg = c;
+    s->variant = c.variant;
+    if (cfg && cfg->batch_us > 0) s->batch_us = cfg->batch_us;
+    if (cfg && cfg->slice_us > 0) s->slice_us = cfg->slice_us;
+    // batch-kernel scratch: the largest per-warp table over the loaded keys
+    size_t warp_words = 1;
+    {
+      std::lock_guard<std::mutex> lk(ctx->mu);
+      for (auto& kv : ctx->keys) {
+        const KeyRec& k = *kv.second;
+        warp_words = std::max(warp_words, (size_t)(32 / hg::tpi_for(k.S, c.variant)) * ((size_t)1 << (k.wm - 1)) * k.S);
+        if (k.secret)
+          warp_words = std::max(warp_words, (size_t)(32 / (2 * hg::tp_for(k.Sp, c.variant))) * 2 *
+                                                ((size_t)1 << (k.sc.wd - 1)) * k.Sp);
+      }
+    }
+    const size_t scratch = (size_t)hg::batch_resident_blocks(c.variant) * hg::batch_warps_per_block() * warp_words * 4;
+    const size_t arena = c.budget_bytes / (size_t)c.slots;
+    for (int i = 0; i < c.slots; ++i) {
+      auto sl = std::make_unique<Slot>();
+      cuda_check(cudaStreamCreateWithFlags(&sl->st, cudaStreamNonBlocking), "stream");
+      cuda_check(cudaEventCreateWithFlags(&sl->ev, cudaEventDisableTiming), "event");
+      sl->dev.base = sl->dev_mem.ensure<uint8_t>(arena);
+      sl->dev.cap = arena;
+      sl->pin.base = sl->pin_mem.ensure<uint8_t>((size_t)16 << 20);
+      sl->pin.cap = (size_t)16 << 20;
+      sl->scratch.ensure<uint32_t>(scratch);
+      sl->counter.ensure<uint32_t>(4);
+      sl->err.ensure<uint32_t>(4);
+      s->slots.push_back(std::move(sl));
+    }
+    hg_server* raw = s.get();
+    s->sched = std::thread(scheduler, raw);
+    *out = s.release();
+    return HG_OK;
+  });
+}
+
+int hg_server_destroy(hg_server* s) {
+  return guarded([&] {
+    if (!s) return HG_OK;
+    {
+      std::lock_guard<std::mutex> lk(s->mu);
+      s->stop = true;
+    }
+    s->cv_work.notify_all();
+    if (s->sched.joinable()) s->sched.join();
+    cudaSetDevice(s->ctx->device);
+    for (auto& sl : s->slots) {
+      cudaStreamSynchronize(sl->st);
+      cudaStreamDestroy(sl->st);
+      cudaEventDestroy(sl->ev);
+    }
+    delete s;
+    return HG_OK;
+  });
+}
+
+int hg_server_store(hg_server* s, int key_id, const uint32_t* host_ct, size_t count, uint64_t* handle) {
+  return guarded([&] {
+    if (!s || !host_ct || !handle || count == 0) fail(HG_ERR_INVALID, "null argument");
+    KeyRec* k = get_key(s->ctx, key_id);
+    set_device(s->ctx);
+    auto r = std::make_unique<Resident>();
+    r->key_id = key_id;
+    r->count = count;
+    void* d = r->buf.ensure<void>(count * (size_t)k->S * 4);
+    cuda_check(cudaMemcpy(d, host_ct, count * (size_t)k->S * 4, cudaMemcpyHostToDevice), "H2D resident");
+    std::lock_guard<std::mutex> lk(s->mu);
+    *handle = s->next_handle++;
+    s->residents[*handle] = std::move(r);
+    return HG_OK;
+  });
+}
+
+int hg_server_release(hg_server* s, uint64_t handle) {
+  return guarded([&] {
+    if (!s) fail(HG_ERR_INVALID, "null server");
+    std::unique_lock<std::mutex> lk(s->mu);
+    // no request in flight may still read it
+    s->cv_done.wait(lk, [&] { return s->pending.empty() && s->inflight == 0; });
+    if (!s->residents.erase(handle)) fail(HG_ERR_INVALID, "unknown resident vector handle");
+    return HG_OK;
+  });
+}
+
+int hg_server_submit(hg_server* s, const hg_request* req, uint64_t* ticket) {
+  return guarded([&] {
+    if (!s || !req || !ticket) fail(HG_ERR_INVALID, "null argument");
+    if (req->op < hg::kBatchEncrypt || req->op > kOpSum) fail(HG_ERR_INVALID, "unknown request op");
+    if (req->count == 0) fail(HG_ERR_INVALID, "empty request");
+    if (!req->out) fail(HG_ERR_INVALID, "request without an output buffer");
+    KeyRec* k = get_key(s->ctx, req->key_id);
+    if (req->op == hg::kBatchDecrypt && !k->secret) fail(HG_ERR_NO_SECRET, "decrypt request on a public key");
+    if ((req->op == hg::kBatchEncrypt || req->op == hg::kBatchMul) && (!req->in0 && !req->h0))
+      fail(HG_ERR_INVALID, "request without input");
+    if (req->op == hg::kBatchMul && !req->in1) fail(HG_ERR_INVALID, "mul request without scalars");
+    if (req->op == hg::kBatchEncrypt && !req->in1) fail(HG_ERR_INVALID, "encrypt request without r");
+    auto q = std::make_unique<Req>();
+    q->r = *req;
+    q->k = k;
+    // the smallest slice must fit a slot (sums are never sliced)
+    q->dev_bytes = slice_dev_bytes(*k, *req, req->op == kOpSum ? req->count : 1);
+    if (q->dev_bytes > s->slots[0]->dev.cap) fail(HG_ERR_NOMEM, "request larger than a server slot");
+    q->t_sub = std::chrono::steady_clock::now();
+    {
+      std::lock_guard<std::mutex> lk(s->mu);
+      if (req->h0 && !s->residents.count(req->h0)) fail(HG_ERR_INVALID, "unknown resident vector handle");
+      if (req->h1 && !s->residents.count(req->h1)) fail(HG_ERR_INVALID, "unknown resident vector handle");
+      q->id = s->next_id++;
+      *ticket = q->id;
+      s->pending.push_back(q.get());
+      s->reqs[q->id] = std::move(q);
+    }
+    s->cv_work.notify_one();
+    return HG_OK;
+  });
+}
+
+int hg_server_wait(hg_server* s, uint64_t ticket, double* latency_s) {
+  int status = HG_OK;
+  const int rc = guarded([&] {
+    if (!s) fail(HG_ERR_INVALID, "null server");
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto it = s->reqs.find(ticket);
+    if (it == s->reqs.end()) fail(HG_ERR_INVALID, "unknown ticket");
+    Req* q = it->second.get();
+    s->cv_done.wait(lk, [&] { return q->done; });
+    if (latency_s) latency_s[0] = std::chrono::duration<double>(q->t_done - q->t_sub).count();
+    status = q->status;
+    s->reqs.erase(it);
+    return HG_OK;
+  });
+  if (rc != HG_OK) return rc;
+  if (status != HG_OK) g_last_error = "request failed";
+  return status;
+}
+
+int hg_server_stats(hg_server* s, uint64_t* completed, uint64_t* batches, size_t* inflight_bytes, size_t* pending) {
+  return guarded([&] {
+    if (!s) fail(HG_ERR_INVALID, "null server");
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (completed) *completed = s->completed;
+    if (batches) *batches = s->batches;
+    if (inflight_bytes) *inflight_bytes = s->inflight;
+    if (pending) *pending = s->pending.size();
+    return HG_OK;
+  });
+}
+
+int hg_probe_serve_load(hg_server* s, const hg_load_spec* spec, double* latencies, int* ops, uint64_t* lens,
+                        double* wall_s) {
+  return guarded([&] {
+    if (!s || !spec || !latencies) fail(HG_ERR_INVALID, "null argument");
+    std::mt19937_64 rng(spec->seed);
+    std::exponential_distribution<double> gap(spec->rate);
+    std::uniform_real_distribution<double> u01(0.0, 1.0);
+    std::discrete_distribution<int> opd(spec->op_weights, spec->op_weights + 5);
+    const double lmin = std::log((double)spec->len_min), lmax = std::log((double)spec->len_max + 1.0);
+    std::vector<uint64_t> tickets(spec->nreq);
+    const auto t0 = std::chrono::steady_clock::now();
+    double t_next = 0.0;
+    static const int op_map[5] = {hg::kBatchEncrypt, hg::kBatchAdd, hg::kBatchMul, kOpSum, hg::kBatchDecrypt};
+    for (size_t i = 0; i < spec->nreq; ++i) {
+      t_next += gap(rng);
+      while (std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count() < t_next) {
+      }
+      const int ki = (int)(rng() % (uint64_t)spec->nkeys);
+      size_t len = (size_t)std::floor(std::exp(lmin + (lmax - lmin) * u01(rng)));
+      len = std::min(std::max(len, spec->len_min), spec->len_max);
+      const int op = op_map[opd(rng)];
+      hg_request r{};
+      r.key_id = spec->key_ids[ki];
+      r.op = op;
+      r.count = len;
+      r.out = spec->sink;
+      if (op == hg::kBatchEncrypt) {
+        r.in0 = spec->m_host;
+        r.in1 = spec->r_host;
+      } else if (op == hg::kBatchMul) {
+        r.h0 = spec->handles[ki];
+        r.in1 = spec->k_host;
+      } else if (op == hg::kBatchAdd) {
+        r.h0 = spec->handles[ki];
+        r.h1 = spec->handles[ki];
+      } else {
+        r.h0 = spec->handles[ki];
+      }
+      const int rc = hg_server_submit(s, &r, &tickets[i]);
+      if (rc != HG_OK) fail(rc, g_last_error);
+      if (ops) ops[i] = op;
+      if (lens) lens[i] = len;
+    }
+    for (size_t i = 0; i < spec->nreq; ++i) {
+      const int rc = hg_server_wait(s, tickets[i], &latencies[i]);
+      if (rc != HG_OK) fail(rc, "served request failed");
+    }
+    if (wall_s) *wall_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return HG_OK;
+  });
+}
 
 int hg_probe_launch_count(uint64_t* out) {
   if (!out) return HG_ERR_INVALID;

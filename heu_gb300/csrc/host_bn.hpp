@@ -291,6 +291,131 @@ class BN {
   }
 };
 
+
+// Montgomery form of the inverse of a Montgomery residue, for the root of
+// the batch-inversion trees: given xr = X*R mod N (N odd, R = 2^(32*S)),
+// returns X^-1 * R mod N as S 32-bit limbs, or false if gcd(X, N) != 1.
+// Kaliski's almost Montgomery inverse ("The Montgomery inverse and its
+// applications", IEEE Trans. Computers 1995) computes w = xr^-1 * 2^k with
+// shifts and adds only; then X^-1 * R = w * 2^(2*32*S - k) mod N.  Runs of
+// zero bits are shifted out at once and the working lengths shrink / grow
+// with the operands.
+inline bool mont_root_inverse(const uint32_t* xr, const BN& N, size_t S, uint32_t* out) {
+  const size_t n = (S + 1) / 2 + 1;  // 64-bit words with one word of slack
+  std::vector<uint64_t> u(n, 0), v(n, 0), r(n + 1, 0), s(n + 1, 0);
+  for (size_t i = 0; i < S; ++i) v[i / 2] |= (uint64_t)xr[i] << (32 * (i % 2));
+  for (size_t i = 0; i < N.d.size(); ++i) u[i / 2] |= (uint64_t)N.d[i] << (32 * (i % 2));
+  auto len_of = [](const std::vector<uint64_t>& a, size_t hint) {
+    while (hint > 0 && a[hint - 1] == 0) --hint;
+    return hint;
+  };
+  auto ctz64 = [](uint64_t x) {
+    int c = 0;
+    while (!(x & 1)) {
+      x >>= 1;
+      ++c;
+    }
+    return c;
+  };
+  // a >>= t (t < 64) over len words
+  auto shr = [](std::vector<uint64_t>& a, size_t len, int t) {
+    if (t == 0) return;
+    for (size_t i = 0; i + 1 < len; ++i) a[i] = (a[i] >> t) | (a[i + 1] << (64 - t));
+    a[len - 1] >>= t;
+  };
+  // a <<= t (t < 64) over len words (len includes room for the carry-out)
+  auto shl = [](std::vector<uint64_t>& a, size_t len, int t) {
+    if (t == 0) return;
+    for (size_t i = len - 1; i > 0; --i) a[i] = (a[i] << t) | (a[i - 1] >> (64 - t));
+    a[0] <<= t;
+  };
+  auto cmp = [](const std::vector<uint64_t>& a, const std::vector<uint64_t>& b, size_t len) {
+    for (size_t i = len; i-- > 0;)
+      if (a[i] != b[i]) return a[i] < b[i] ? -1 : 1;
+    return 0;
+  };
+  auto sub = [](std::vector<uint64_t>& a, const std::vector<uint64_t>& b, size_t len) {
+    uint64_t br = 0;
+    for (size_t i = 0; i < len; ++i) {
+      const uint64_t ai = a[i], bi = b[i];
+      a[i] = ai - bi - br;
+      br = (ai < bi) | ((ai == bi) & br);
+    }
+  };
+  auto add = [](std::vector<uint64_t>& a, const std::vector<uint64_t>& b, size_t len) {
+    uint64_t c = 0;
+    for (size_t i = 0; i < len; ++i) {
+      const uint64_t t = a[i] + c;
+      const uint64_t c1 = t < c;
+      a[i] = t + b[i];
+      c = c1 | (a[i] < t);
+    }
+  };
+  s[0] = 1;
+  size_t luv = n, lrs = 1;
+  size_t k = 0;
+  luv = std::max(len_of(u, n), len_of(v, n));
+  if (luv == 0) return false;
+  while (true) {
+    const size_t lv = len_of(v, luv);
+    if (lv == 0) break;
+    if (!(u[0] & 1)) {
+      int t = 0;
+      while (u[0] == 0) {  // whole zero words
+        for (size_t i = 0; i + 1 < luv; ++i) u[i] = u[i + 1];
+        u[luv - 1] = 0;
+        for (size_t i = lrs + 1; i-- > 1;) s[i] = s[i - 1];
+        s[0] = 0;
+        lrs = std::min(lrs + 1, n);
+        k += 64;
+      }
+      t = ctz64(u[0]);
+      shr(u, luv, t);
+      lrs = std::min(lrs + 1, n);
+      shl(s, lrs + 1, t);
+      k += (size_t)t;
+    } else if (!(v[0] & 1)) {
+      int t = 0;
+      while (v[0] == 0) {
+        for (size_t i = 0; i + 1 < luv; ++i) v[i] = v[i + 1];
+        v[luv - 1] = 0;
+        for (size_t i = lrs + 1; i-- > 1;) r[i] = r[i - 1];
+        r[0] = 0;
+        lrs = std::min(lrs + 1, n);
+        k += 64;
+      }
+      t = ctz64(v[0]);
+      shr(v, luv, t);
+      lrs = std::min(lrs + 1, n);
+      shl(r, lrs + 1, t);
+      k += (size_t)t;
+    } else if (cmp(u, v, luv) > 0) {
+      sub(u, v, luv);
+      add(r, s, lrs + 1);
+    } else {
+      sub(v, u, luv);
+      add(s, r, lrs + 1);
+    }
+    luv = std::max<size_t>(1, std::max(len_of(u, luv), len_of(v, luv)));
+    lrs = std::max(len_of(r, lrs + 1), len_of(s, lrs + 1));
+  }
+  // gcd is u; invertible only if u == 1
+  if (!(u[0] == 1 && len_of(u, luv) == 1)) return false;
+  // w = N - (r mod N)
+  std::vector<uint32_t> rw(2 * (n + 1));
+  for (size_t i = 0; i < n + 1; ++i) {
+    rw[2 * i] = (uint32_t)r[i];
+    rw[2 * i + 1] = (uint32_t)(r[i] >> 32);
+  }
+  BN rb = BN::from_limbs(rw.data(), rw.size()) % N;
+  const BN w = rb.is_zero() ? BN() : N - rb;
+  const size_t two_bits = 2 * 32 * S;
+  if (k > two_bits) return false;
+  const BN z = w.shl(two_bits - k) % N;
+  z.to_limbs(out, S);
+  return true;
+}
+
 // Montgomery context over an odd modulus with 32-bit limbs, used by the
 // Miller-Rabin test during key generation (many modexps).
 class HostMont {

@@ -185,19 +185,6 @@ __global__ void __launch_bounds__(kBlock) k_tree_apply(KeyConst kc, const uint32
   store_slice<L>(out + inst * S + g.t * L, A);
 }
 
-// root_slot = MM(z, R^3) where z = (X*R)^-1 mod N, giving X^-1 * R.
-template <int TPI, int L>
-__global__ void __launch_bounds__(32) k_root_fix(KeyConst kc, const uint32_t* __restrict__ z,
-                                                 uint32_t* __restrict__ root_slot) {
-  const Group<TPI> g;
-  uint32_t N[L], A[L], B[L];
-  load_slice<L>(N, kc.N + g.t * L);
-  load_slice<L>(A, z + g.t * L);
-  load_slice<L>(B, kc.R3 + g.t * L);
-  mont_mul<TPI, L>(A, A, B, N, kc.np, g);
-  if (threadIdx.x < TPI) store_slice<L>(root_slot + g.t * L, A);
-}
-
 // ---------------------------------------------------------------------------
 // Fixed-base table (public_key.cc:28-40 builds yacl's BaseTable on the host):
 //   bases[pos] = h_s^(2^(w*pos)) (one group, sequential squarings)
@@ -375,12 +362,6 @@ cudaError_t launch_tree_apply(int S, const KeyConst& kc, const uint32_t* in, con
   HG_DISPATCH_S0(S,
                  k_tree_apply<TPI, L><<<blocks_for(count, TPI), kBlock, 0, st>>>(kc, in, sel, leaves_inv, out,
                                                                                  count));
-  return counted();
-}
-
-cudaError_t launch_root_fix(int S, const KeyConst& kc, const uint32_t* root_inv_z, uint32_t* root_slot,
-                            cudaStream_t st) {
-  HG_DISPATCH_S0(S, k_root_fix<TPI, L><<<1, 32, 0, st>>>(kc, root_inv_z, root_slot));
   return counted();
 }
 

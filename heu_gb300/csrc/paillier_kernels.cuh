@@ -84,8 +84,6 @@ cudaError_t launch_tree_down(int S, const KeyConst& kc, uint32_t* lower, const u
                              size_t upper_count, cudaStream_t st);
 cudaError_t launch_tree_apply(int S, const KeyConst& kc, const uint32_t* in, const int64_t* sel,
                               const uint32_t* leaves_inv, uint32_t* out, size_t count, cudaStream_t st);
-cudaError_t launch_root_fix(int S, const KeyConst& kc, const uint32_t* root_inv_z, uint32_t* root_slot,
-                            cudaStream_t st);
 // fixed-base table construction
 cudaError_t launch_table_bases(int S, const KeyConst& kc, const uint32_t* hs_mont, uint32_t* bases,
                                cudaStream_t st);

@@ -1,0 +1,403 @@
+// Continuous-batching request server (hg_server_* of the C-ABI).
+//
+// Included into engine.cu's translation unit: it uses the engine's key
+// records, inversion tasks and batch planner.
+//
+// A scheduler thread owns `slots` in-flight micro-batches, each with its own
+// stream, a device arena, a pinned arena and a scratch buffer for the
+// persistent batch kernel, all sized when the server starts so nothing is
+// allocated while serving.  Requests wait in a FIFO; whenever a slot is free
+// the scheduler admits requests from the front while their device bytes fit
+// the slot's arena and the server-wide budget, stages their host inputs,
+// runs all their encrypt / decrypt / add / mul work in one persistent launch
+// (sums as reduction levels, negative scalars as product trees with a host
+// inversion node), copies the results back and records an event.  Requests
+// that arrive meanwhile are admitted into the next free slot while earlier
+// slots are still on the GPU, so their work overlaps on the device.
+
+namespace {
+
+constexpr int kOpSum = 4;  // server-only op on top of the batch ops
+
+struct Arena {
+  uint8_t* base = nullptr;
+  size_t cap = 0, off = 0;
+  void reset() { off = 0; }
+  bool fits(size_t bytes) const { return off + ((bytes + 255) & ~size_t(255)) <= cap; }
+  template <typename T>
+  T* take(size_t bytes) {
+    const size_t a = (bytes + 255) & ~size_t(255);
+    if (off + a > cap) fail(HG_ERR_NOMEM, "server arena exhausted");
+    T* p = reinterpret_cast<T*>(base + off);
+    off += a;
+    return p;
+  }
+};
+
+struct Resident {
+  int key_id;
+  size_t count;
+  DevBuf buf;
+};
+
+struct Req {
+  hg_request r;
+  KeyRec* k = nullptr;
+  uint64_t id = 0;
+  size_t dev_bytes = 0;
+  std::chrono::steady_clock::time_point t_sub, t_done;
+  int status = HG_OK;
+  bool done = false;
+  InvTask* task = nullptr;
+  const void* p0 = nullptr;  // resolved resident vectors (set at admission, under the lock)
+  const void* p1 = nullptr;
+  size_t next = 0;         // first element not yet handed to a micro-batch
+  int outstanding = 0;     // slices on the GPU
+  std::vector<std::unique_ptr<InvTask>> tasks;
+};
+
+// A contiguous slice [start, start + len) of one request.
+struct Slice {
+  Req* q;
+  size_t start, len;
+  size_t bytes;
+  InvTask* task;
+};
+
+struct Slot {
+  cudaStream_t st = nullptr;
+  cudaEvent_t ev = nullptr;
+  DevBuf dev_mem, scratch, counter, err;
+  PinBuf pin_mem;
+  Arena dev, pin;
+  std::vector<Slice> slices;
+  size_t bytes = 0;
+  uint32_t* err_host = nullptr;
+  bool busy = false;
+};
+
+size_t slice_dev_bytes(const KeyRec& k, const hg_request& r, size_t n) {
+  const size_t cb = (size_t)k.S * 4, pad = 256;
+  const size_t tree = 2 * padded_pow2(n) * cb + cb + pad;
+  switch (r.op) {
+    case hg::kBatchEncrypt: return n * 8 + n * (size_t)k.kc.rlimbs * 4 + n * cb + 3 * pad;
+    case hg::kBatchDecrypt: return (r.h0 ? 0 : n * cb) + n * 9 + 3 * pad;
+    case hg::kBatchAdd: return (r.h0 ? 0 : n * cb) + (r.h1 ? 0 : n * cb) + n * cb + 3 * pad;
+    case hg::kBatchMul: return (r.h0 ? 0 : n * cb) + n * 8 + n * cb + tree + 3 * pad;
+    case kOpSum: return (r.h0 ? 0 : n * cb) + 2 * ((n + 1) / 2) * cb + cb + 4 * pad;
+    default: return 0;
+  }
+}
+
+// Estimated GPU time of one element of an op, in microseconds (cost model
+// used to size micro-batches; the kernels do not depend on it).
+double elem_cost_us(const KeyRec& k, int op) {
+  if (op == kOpSum) return (double)k.S * k.S / 3.11e6;
+  return job_cost(k, op) / 3.11e6;
+}
+
+}  // namespace
+
+struct hg_server {
+  hg_ctx* ctx = nullptr;
+  hg_server_config cfg{};
+  std::vector<std::unique_ptr<Slot>> slots;
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  std::deque<Req*> pending;
+  std::unordered_map<uint64_t, std::unique_ptr<Req>> reqs;
+  std::unordered_map<uint64_t, std::unique_ptr<Resident>> residents;
+  uint64_t next_id = 1, next_handle = 1;
+  size_t inflight = 0;
+  uint64_t completed = 0, batches = 0;
+  bool stop = false;
+  int variant = 0;
+  double batch_us = 100000.0;  // target GPU time of one micro-batch
+  double slice_us = 50000.0;   // most GPU time one request gets per micro-batch
+  std::thread sched;
+};
+
+namespace {
+
+const void* resident_ptr(hg_server& s, uint64_t h, const KeyRec& k, size_t count) {
+  auto it = s.residents.find(h);
+  if (it == s.residents.end()) fail(HG_ERR_INVALID, "unknown resident vector handle");
+  if (it->second->count < count) fail(HG_ERR_INVALID, "request longer than its resident vector");
+  if (it->second->key_id < 0 || get_key(s.ctx, it->second->key_id) != &k)
+    fail(HG_ERR_INVALID, "resident vector belongs to another key");
+  return it->second->buf.p;
+}
+
+// Stage and enqueue one micro-batch on its slot (scheduler thread, no lock).
+void run_slot(hg_server& s, Slot& sl) {
+  sl.dev.reset();
+  sl.pin.reset();
+  cudaStream_t st = sl.st;
+  std::vector<JobSpec> specs;
+  struct Post {
+    Req* q;
+    const void* dev_out;
+    size_t bytes;
+    const void* dev_aux;
+    size_t aux_bytes;
+    size_t out_off, aux_off;  // byte offsets of the slice in the host buffers
+  };
+  std::vector<Post> posts;
+  struct SumJob {
+    Req* q;
+    const uint32_t* src;
+    uint32_t* bufs[2];
+    uint32_t* out;
+  };
+  std::vector<SumJob> sums;
+  struct InvJob {
+    Req* q;
+    KeyRec* k;
+    uint32_t* data;
+    const int64_t* sel;
+    size_t count;
+    uint32_t* tree;
+    InvTask* task;
+  };
+  std::vector<InvJob> invs;
+  uint32_t* err = sl.err.as<uint32_t>();
+  cuda_check(cudaMemsetAsync(err, 0, 4, st), "memset err");
+  for (Slice& sc : sl.slices) {
+    Req* q = sc.q;
+    const hg_request& r = q->r;
+    KeyRec& k = *q->k;
+    const size_t n = sc.len, cb = (size_t)k.S * 4, s0 = sc.start;
+    auto h2d_in = [&](const void* host, size_t bytes) {
+      void* d = sl.dev.take<void>(bytes);
+      cuda_check(cudaMemcpyAsync(d, host, bytes, cudaMemcpyHostToDevice, st), "H2D");
+      return d;
+    };
+    auto at = [](const void* p, size_t off) -> const void* { return static_cast<const uint8_t*>(p) + off; };
+    auto ct_in = [&](const void* resident, const void* host) -> const void* {
+      return resident ? at(resident, s0 * cb) : h2d_in(at(host, s0 * cb), n * cb);
+    };
+    if (r.op == hg::kBatchEncrypt) {
+      const void* m = h2d_in(at(r.in0, s0 * 8), n * 8);
+      const size_t rb = (size_t)k.kc.rlimbs * 4;
+      const void* rr = h2d_in(at(r.in1, s0 * rb), n * rb);
+      void* out = sl.dev.take<void>(n * cb);
+      specs.push_back({&k, r.op, 0, n, m, rr, out, nullptr});
+      posts.push_back({q, out, n * cb, nullptr, 0, s0 * cb, 0});
+    } else if (r.op == hg::kBatchDecrypt) {
+      const void* c = ct_in(q->p0, r.in0);
+      void* out = sl.dev.take<void>(n * 8);
+      void* ovf = sl.dev.take<void>(n);
+      specs.push_back({&k, r.op, 0, n, c, nullptr, out, ovf});
+      posts.push_back({q, out, n * 8, r.aux ? ovf : nullptr, r.aux ? n : 0, s0 * 8, s0});
+    } else if (r.op == hg::kBatchAdd) {
+      const void* a = ct_in(q->p0, r.in0);
+      const void* b = ct_in(q->p1, r.in1);
+      void* out = sl.dev.take<void>(n * cb);
+      specs.push_back({&k, r.op, 0, n, a, b, out, nullptr});
+      posts.push_back({q, out, n * cb, nullptr, 0, s0 * cb, 0});
+    } else if (r.op == hg::kBatchMul) {
+      const void* a = ct_in(q->p0, r.in0);
+      const int64_t* hk = static_cast<const int64_t*>(r.in1) + s0;
+      bool neg = false;
+      for (size_t i = 0; i < n && !neg; ++i) neg = hk[i] < 0;
+      const void* kk = h2d_in(hk, n * 8);
+      auto* out = sl.dev.take<uint32_t>(n * cb);
+      specs.push_back({&k, r.op, neg ? 0 : HG_JOB_NONNEG, n, a, kk, out, nullptr});
+      if (neg) {
+        InvTask* task = sc.task;
+        task->root = sl.pin.take<uint32_t>(cb + 4);
+        task->z = sl.pin.take<uint32_t>(cb);
+        const size_t padded = padded_pow2(n);
+        invs.push_back({q, &k, out, static_cast<const int64_t*>(kk), n, sl.dev.take<uint32_t>(2 * padded * cb),
+                        task});
+      }
+      posts.push_back({q, out, n * cb, nullptr, 0, s0 * cb, 0});
+    } else {  // sum
+      const auto* src = static_cast<const uint32_t*>(ct_in(q->p0, r.in0));
+      const size_t half = (n + 1) / 2;
+      SumJob sj{q, src, {sl.dev.take<uint32_t>(half * cb), sl.dev.take<uint32_t>(half * cb)},
+                sl.dev.take<uint32_t>(cb)};
+      sums.push_back(sj);
+      posts.push_back({q, sj.out, cb, nullptr, 0, 0, 0});
+    }
+  }
+  if (!specs.empty()) {
+    const BatchPlan plan = plan_batch(specs, s.variant);
+    const size_t jb = plan.jobs.size() * sizeof(hg::BatchJob), tb = plan.tiles.size() * sizeof(hg::BatchTile);
+    auto* hj = sl.pin.take<uint8_t>(jb);
+    auto* ht = sl.pin.take<uint8_t>(tb);
+    std::memcpy(hj, plan.jobs.data(), jb);
+    std::memcpy(ht, plan.tiles.data(), tb);
+    auto* dj = sl.dev.take<hg::BatchJob>(jb);
+    auto* dt = sl.dev.take<hg::BatchTile>(tb);
+    cuda_check(cudaMemcpyAsync(dj, hj, jb, cudaMemcpyHostToDevice, st), "H2D jobs");
+    cuda_check(cudaMemcpyAsync(dt, ht, tb, cudaMemcpyHostToDevice, st), "H2D tiles");
+    cuda_check(cudaMemsetAsync(sl.counter.p, 0, 4, st), "memset counter");
+    const int grid = hg::batch_resident_blocks(s.variant);
+    if ((size_t)grid * hg::batch_warps_per_block() * plan.warp_words * 4 > sl.scratch.n)
+      fail(HG_ERR_NOMEM, "server scratch too small for this batch");
+    cuda_check(hg::launch_batch(s.variant, dj, dt, (uint32_t)plan.tiles.size(), sl.counter.as<uint32_t>(),
+                                sl.scratch.as<uint32_t>(), plan.warp_words, err, grid, st),
+               "batch launch");
+  }
+  for (auto& iv : invs) {
+    iv.task->status = 0;
+    core_inverse_async_raw(*iv.k, iv.data, iv.sel, iv.data, iv.count, iv.tree, *iv.task, err, st);
+  }
+  for (auto& sj : sums) {
+    KeyRec& k = *sj.q->k;
+    size_t n = sj.q->r.count;  // sums are never sliced
+    const uint32_t* cur = sj.src;
+    int which = 0;
+    if (n == 1) {
+      cuda_check(cudaMemcpyAsync(sj.out, cur, (size_t)k.S * 4, cudaMemcpyDeviceToDevice, st), "copy");
+    }
+    while (n > 1) {
+      const int chunk = (int)std::min<size_t>(64, std::max<size_t>(2, (n + 4095) / 4096));
+      const size_t on = (n + chunk - 1) / chunk;
+      uint32_t* dst = on == 1 ? sj.out : sj.bufs[which];
+      cuda_check(hg::launch_reduce(k.S, k.kc, cur, n, chunk, dst, err, st), "reduce");
+      cur = dst;
+      n = on;
+      which ^= 1;
+    }
+  }
+  for (auto& p : posts) {
+    cuda_check(cudaMemcpyAsync(static_cast<uint8_t*>(p.q->r.out) + p.out_off, p.dev_out, p.bytes,
+                               cudaMemcpyDeviceToHost, st),
+               "D2H");
+    if (p.dev_aux)
+      cuda_check(cudaMemcpyAsync(static_cast<uint8_t*>(p.q->r.aux) + p.aux_off, p.dev_aux, p.aux_bytes,
+                                 cudaMemcpyDeviceToHost, st),
+                 "D2H");
+  }
+  sl.err_host = sl.pin.take<uint32_t>(4);
+  cuda_check(cudaMemcpyAsync(sl.err_host, err, 4, cudaMemcpyDeviceToHost, st), "D2H err");
+  cuda_check(cudaEventRecord(sl.ev, st), "event");
+}
+
+void finish_req(hg_server& s, Req* q) {
+  q->done = true;
+  q->t_done = std::chrono::steady_clock::now();
+  ++s.completed;
+  s.cv_done.notify_all();
+}
+
+void scheduler(hg_server* sp) {
+  hg_server& s = *sp;
+  cudaSetDevice(s.ctx->device);
+  std::unique_lock<std::mutex> lk(s.mu);
+  while (true) {
+    // retire finished slots
+    for (auto& slp : s.slots) {
+      Slot& sl = *slp;
+      if (!sl.busy) continue;
+      if (cudaEventQuery(sl.ev) != cudaSuccess) continue;
+      const uint32_t bits = *sl.err_host;
+      for (Slice& sc : sl.slices) {
+        Req* q = sc.q;
+        if (bits & hg::kErrCtRange) q->status = HG_ERR_CT_RANGE;
+        if (sc.task && sc.task->status == 1 && q->status == HG_OK) q->status = HG_ERR_NOT_INVERTIBLE;
+        if (sc.task && sc.task->status == 2) q->status = HG_ERR_CT_RANGE;
+        if (--q->outstanding == 0 && q->next == q->r.count) finish_req(s, q);
+      }
+      s.inflight -= sl.bytes;
+      sl.slices.clear();
+      sl.busy = false;
+    }
+    if (s.stop && s.pending.empty()) {
+      bool any = false;
+      for (auto& slp : s.slots) any |= slp->busy;
+      if (!any) break;
+    }
+    // admit: every pending request gets a slice of at most slice_us of work
+    // per micro-batch (processor sharing), until the batch reaches batch_us
+    bool launched = false;
+    for (auto& slp : s.slots) {
+      Slot& sl = *slp;
+      if (sl.busy || s.pending.empty()) continue;
+      size_t elems = 0, bytes = 0;
+      double cost = 0.0;
+      for (auto it = s.pending.begin(); it != s.pending.end();) {
+        Req* q = *it;
+        if (q->next == 0 && q->outstanding == 0 && !q->p0 && !q->p1 && (q->r.h0 || q->r.h1)) {
+          try {
+            q->p0 = q->r.h0 ? resident_ptr(s, q->r.h0, *q->k, q->r.count) : nullptr;
+            q->p1 = q->r.h1 ? resident_ptr(s, q->r.h1, *q->k, q->r.count) : nullptr;
+          } catch (const HgError& e) {
+            q->status = e.code;
+            q->next = q->r.count;
+            it = s.pending.erase(it);
+            if (q->outstanding == 0) finish_req(s, q);
+            continue;
+          }
+        }
+        const double cpe = elem_cost_us(*q->k, q->r.op);
+        const size_t remain = q->r.count - q->next;
+        size_t len = remain;
+        if (q->r.op != kOpSum) {
+          const size_t cap = (size_t)std::max(1.0, s.slice_us / std::max(cpe, 1e-9));
+          len = std::min(len, std::max<size_t>(cap, 1));
+          len = std::min(len, s.cfg.max_batch_elems);
+        }
+        const size_t need = slice_dev_bytes(*q->k, q->r, len);
+        const bool first = sl.slices.empty();
+        if (!first && (elems + len > s.cfg.max_batch_elems || bytes + need > sl.dev.cap ||
+                       s.inflight + bytes + need > s.cfg.budget_bytes || cost >= s.batch_us))
+          break;
+        if (first && s.inflight + need > s.cfg.budget_bytes && s.inflight > 0) break;  // wait for memory
+        std::unique_ptr<InvTask> task;
+        InvTask* tp = nullptr;
+        if (q->r.op == hg::kBatchMul) {
+          task = std::make_unique<InvTask>();
+          tp = task.get();
+          q->tasks.push_back(std::move(task));
+        }
+        sl.slices.push_back({q, q->next, len, need, tp});
+        q->next += len;
+        q->outstanding++;
+        elems += len;
+        bytes += need;
+        cost += cpe * (double)len;
+        if (q->next == q->r.count)
+          it = s.pending.erase(it);
+        else
+          ++it;
+      }
+      if (sl.slices.empty()) continue;
+      s.inflight += bytes;
+      sl.bytes = bytes;
+      sl.busy = true;
+      ++s.batches;
+      lk.unlock();
+      try {
+        run_slot(s, sl);
+      } catch (const HgError& e) {
+        cudaStreamSynchronize(sl.st);
+        lk.lock();
+        for (Slice& sc : sl.slices) {
+          Req* q = sc.q;
+          q->status = e.code;
+          if (--q->outstanding == 0 && q->next == q->r.count) finish_req(s, q);
+        }
+        s.inflight -= bytes;
+        sl.slices.clear();
+        sl.busy = false;
+        lk.unlock();
+      }
+      if (!lk.owns_lock()) lk.lock();
+      launched = true;
+    }
+    if (!launched) {
+      bool any_busy = false;
+      for (auto& slp : s.slots) any_busy |= slp->busy;
+      // poll busy slots quickly; sleep when idle until work arrives
+      if (any_busy)
+        s.cv_work.wait_for(lk, std::chrono::microseconds(20));
+      else
+        s.cv_work.wait_for(lk, std::chrono::milliseconds(5), [&] { return s.stop || !s.pending.empty(); });
+    }
+  }
+}
+
+}  // namespace

@@ -179,6 +179,49 @@ int hg_batch_set_variant(hg_batch* b, int variant);
 int hg_batch_run(hg_batch* b, void* stream, int use_graph);
 int hg_batch_wait(hg_batch* b, void* stream);
 
+/* ---- continuous-batching server (no counterpart in the reference) --------
+ * Keeps the loaded keys' tables and resident ciphertext vectors on the
+ * device and serves requests submitted from any host thread.  A scheduler
+ * thread admits queued requests into free slots (stream + device arena) as
+ * long as their device bytes fit the slot and the server-wide budget, runs
+ * each slot's requests as one persistent batch launch (sums as reduction
+ * levels) and copies results back; requests arriving meanwhile are admitted
+ * into the next free slot while earlier ones are still on the GPU, and
+ * every pending request gets a slice of each micro-batch (processor
+ * sharing).  Each result is bit-identical to the same request run alone.  Configure keys
+ * (hg_key_set_config / hg_autotune) before creating the server.           */
+typedef struct hg_server hg_server;
+#define HG_OP_SUM 4
+typedef struct {
+  size_t budget_bytes;    /* device memory for in-flight requests (0 = 40 GiB) */
+  int slots;              /* concurrent micro-batches (0 = 4); each owns budget/slots */
+  size_t max_batch_elems; /* ciphertexts per micro-batch (0 = 2^20) */
+  int variant;            /* layout variant of the batch kernel, 0 or 1 */
+  double batch_us;        /* estimated GPU time per micro-batch (0 = 100000) */
+  double slice_us;        /* most estimated GPU time one request gets per
+                             micro-batch (0 = 50000); longer requests are cut
+                             into slices so short ones are not stuck behind
+                             them (sums are never cut) */
+} hg_server_config;
+typedef struct {
+  int key_id;
+  int op;           /* HG_OP_ENCRYPT / DECRYPT / ADD / MUL / SUM */
+  size_t count;
+  const void* in0;  /* host: int64 m | ct | ct a | ct a | ct (unused when h0 != 0) */
+  const void* in1;  /* host: r limbs | - | ct b | int64 k | - (ADD: unused when h1) */
+  uint64_t h0, h1;  /* resident vector handles in place of in0 / in1, 0 = none */
+  void* out;        /* host: ct | int64 m | ct | ct | one ct */
+  void* aux;        /* host: - | overflow flags (may be NULL) | - | - | - */
+} hg_request;
+int hg_server_create(hg_ctx* ctx, const hg_server_config* cfg, hg_server** out);
+int hg_server_destroy(hg_server* s);
+int hg_server_store(hg_server* s, int key_id, const uint32_t* host_ct, size_t count, uint64_t* handle);
+int hg_server_release(hg_server* s, uint64_t handle);
+int hg_server_submit(hg_server* s, const hg_request* req, uint64_t* ticket);
+/* Blocks until the request is done; returns its status and releases the ticket. */
+int hg_server_wait(hg_server* s, uint64_t ticket, double* latency_s);
+int hg_server_stats(hg_server* s, uint64_t* completed, uint64_t* batches, size_t* inflight_bytes, size_t* pending);
+
 /* ---- device-pointer forms (asynchronous on `stream`) --------------------
  * Same semantics as the host forms above.  Range errors raised by kernels
  * are collected per context; hg_dev_check(ctx) synchronises and reports

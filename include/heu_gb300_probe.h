@@ -20,6 +20,32 @@ int hg_probe_mac_peak(int device, int pattern, double* macs_per_second, double* 
 /* Number of engine kernels this process has launched so far. */
 int hg_probe_launch_count(uint64_t* out);
 
+/* Open-loop load generator for the request server: Poisson arrivals at
+ * `rate`/s, lengths log-uniform in [len_min, len_max], keys uniform over
+ * key_ids, ops drawn with op_weights over (encrypt, add, mul, sum, decrypt);
+ * add / mul / sum / decrypt read the key's resident vector handles[i],
+ * encrypt reads m_host / r_host, mul reads k_host; every result goes to
+ * `sink` (a timing sink, overwritten).  Fills latencies[nreq] (seconds),
+ * ops and lens, and the wall time from the first arrival to the last
+ * completion. */
+typedef struct hg_server hg_server;
+typedef struct {
+  const int* key_ids;
+  int nkeys;
+  const uint64_t* handles;
+  double rate;
+  size_t nreq;
+  size_t len_min, len_max;
+  double op_weights[5];
+  uint64_t seed;
+  const void* m_host;
+  const void* r_host;
+  const void* k_host;
+  void* sink;
+} hg_load_spec;
+int hg_probe_serve_load(hg_server* s, const hg_load_spec* spec, double* latencies, int* ops, uint64_t* lens,
+                        double* wall_s);
+
 #ifdef __cplusplus
 }
 #endif
