@@ -50,3 +50,38 @@ def gpu_key(gpu_ctx):
         return _GPU_KEYS[k]
 
     return get
+
+
+_SPI_BIN = {}
+
+
+def spi_test_binary():
+    """Builds tests/cpp/spi_test.cpp (the C++ SPI adapter test) with g++
+    against the engine library; returns its path."""
+    import subprocess
+
+    from heu_gb300 import build as hb
+    from heu_gb300 import capi
+
+    capi.load()  # builds the library if it is missing
+    if "bin" not in _SPI_BIN:
+        out_dir = os.path.join(ROOT, "heu_gb300", "_lib")
+        exe = os.path.join(out_dir, "spi_test")
+        lib_dir = os.path.dirname(hb.LIB_PATH)
+        cmd = ["g++", "-std=c++17", "-O2", "-Wall", "-Werror", "-o", exe,
+               os.path.join(ROOT, "tests", "cpp", "spi_test.cpp"), f"-L{lib_dir}", "-lheu_gb300",
+               f"-Wl,-rpath,{lib_dir}"]
+        subprocess.run(cmd, check=True, capture_output=True, text=True)
+        _SPI_BIN["bin"] = exe
+    return _SPI_BIN["bin"]
+
+
+def parse_spi_output(text):
+    """'name value' lines of spi_test into a dict (hex values as ints where
+    they parse)."""
+    out = {}
+    for line in text.splitlines():
+        parts = line.split(" ", 1)
+        if len(parts) == 2 and not line.startswith(("FAIL", "audit")):
+            out[parts[0]] = parts[1]
+    return out

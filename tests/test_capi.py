@@ -58,3 +58,20 @@ def test_limb_helpers_roundtrip():
     arr = hg.ints_to_limbs(vals, 32)
     assert arr.shape == (4, 32) and arr.dtype == np.uint32
     assert hg.limbs_to_ints(arr) == vals
+
+
+def test_cpp_spi_adapter_builds_and_generates_the_oracle_key():
+    """heu_gb300/cpp/paillier_gb300.h compiles as plain C++17 and its
+    KeyGenerator (host only) gives the oracle's key for the same seed."""
+    import subprocess
+
+    from tests.conftest import parse_spi_output, spi_test_binary
+
+    exe = spi_test_binary()
+    res = subprocess.run([exe, "keygen", "1024", "1"], capture_output=True, text=True, timeout=120)
+    assert res.returncode == 0, res.stdout + res.stderr
+    assert res.stdout.strip().endswith("OK")
+    got = parse_spi_output(res.stdout)
+    pk, sk = oracle_key(1024, 1)
+    assert int(got["n"], 16) == pk.n and int(got["p"], 16) == sk.p and int(got["q"], 16) == sk.q
+    assert int(got["h_s"], 16) == pk.h_s
