@@ -280,11 +280,16 @@ inline bool AllInt64(ConstSpan<Plaintext> pts) {
   return true;
 }
 
+// |m| <= n/2 (encryptor.cc:38-40), checked before any r is drawn
+inline void CheckPlaintexts(const PublicKey& pk, ConstSpan<Plaintext> pts) {
+  for (auto* p : pts)
+    if (p->CompareAbs(pk.PlaintextBound()) > 0) throw std::invalid_argument("message number out of range");
+}
+
 // Encrypt plaintexts with the given r limbs (int64 fast path or full range).
 inline std::vector<uint32_t> EncryptLimbs(const PublicKey& pk, ConstSpan<Plaintext> pts, const uint32_t* r) {
   const size_t n = pts.size(), S = pk.Limbs();
-  for (auto* p : pts)
-    if (p->CompareAbs(pk.PlaintextBound()) > 0) throw std::invalid_argument("message number out of range");
+  CheckPlaintexts(pk, pts);
   std::vector<uint32_t> ct(n * S);
   hg_ctx* ctx = Engine::Get().ctx;
   const int id = KeyId(pk, nullptr);
@@ -344,12 +349,14 @@ class Encryptor {
   }
 
   std::vector<Ciphertext> Encrypt(ConstSpan<Plaintext> pts) const {
+    detail::CheckPlaintexts(pk_, pts);
     const auto r = detail::DrawR(pk_, pts.size());
     return detail::ToCts(detail::EncryptLimbs(pk_, pts, r.data()), pk_.Limbs());
   }
 
   // encryptor.cc:51-53 audit string: "p:{m},rn:{h_s^r},c:{c}"
   std::pair<std::vector<Ciphertext>, std::vector<std::string>> EncryptWithAudit(ConstSpan<Plaintext> pts) const {
+    detail::CheckPlaintexts(pk_, pts);
     const auto r = detail::DrawR(pk_, pts.size());
     auto cts = detail::ToCts(detail::EncryptLimbs(pk_, pts, r.data()), pk_.Limbs());
     std::vector<uint32_t> rn(pts.size() * pk_.Limbs());

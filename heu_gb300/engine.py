@@ -165,6 +165,31 @@ class Key:
         capi.check(self.lib.hg_decrypt_bn(self.ctx.handle, self.id, _ptr(ct), _ptr(mag), _ptr(neg), ct.shape[0]))
         return [(-v if s else v) for v, s in zip(limbs_to_ints(mag), neg)]
 
+    def decrypt_in_range(self, ct, range_bits=64):
+        """heu.numpy DecryptInRange (numpy/decryptor.cc:24-47, 86-99): decrypt
+        and raise if any plaintext's magnitude has more than `range_bits` bits.
+        Returns int64 values when range_bits <= 63, Python ints otherwise."""
+        if range_bits <= 63:
+            m, ovf = self.decrypt(ct)
+            lim = 1 << range_bits  # |m| has more than range_bits bits iff |m| >= lim
+            bad = ovf.astype(bool) | (m == np.iinfo(np.int64).min)
+            if range_bits < 63:
+                bad |= (m >= lim) | (m <= -lim)
+            if bad.any():
+                i = int(np.nonzero(bad)[0][0])
+                found = abs(self.decrypt_bn(self._ct(ct)[i:i + 1])[0]).bit_length()
+                raise ValueError("Dangerous!!! HE ciphertext range check failed, there may be a malicious party "
+                                 f"stealing your data, please stop computing immediately. found "
+                                 f"pt.BitCount()={found}, expected {range_bits}")
+            return m
+        vals = self.decrypt_bn(ct)
+        for v in vals:
+            if abs(v).bit_length() > range_bits:
+                raise ValueError("Dangerous!!! HE ciphertext range check failed, there may be a malicious party "
+                                 f"stealing your data, please stop computing immediately. found "
+                                 f"pt.BitCount()={abs(v).bit_length()}, expected {range_bits}")
+        return vals
+
     # -- evaluator --------------------------------------------------------
     def _binary_ct(self, fn, a, b):
         a, b = self._ct(a), self._ct(b)

@@ -135,3 +135,25 @@ def test_config3_matmul_full_size(gpu_key):
     d, ovf = key.decrypt(out.reshape(-1, key.ct_limbs))
     assert ovf.sum() == 0
     assert np.array_equal(d.reshape(M, N), x @ y)
+
+
+def test_decrypt_in_range(gpu_key):
+    """DecryptInRange (numpy/decryptor.cc:24-47): values within range_bits pass,
+    one value with more bits raises with the reference's message."""
+    key, pk, sk = gpu_key(1024, 1)
+    m = np.array([0, 1, -1, 2 ** 20 - 1, -(2 ** 20 - 1), 12345], dtype=np.int64)
+    r = np.zeros((m.size, key.r_limbs), np.uint32)
+    r[:, 0] = np.arange(1, m.size + 1)
+    ct = key.encrypt(m, r)
+    assert np.array_equal(key.decrypt_in_range(ct, 20), m)
+    assert key.decrypt_in_range(ct, 200) == m.tolist()
+    for bad in (2 ** 20, -(2 ** 20)):
+        ct2 = np.concatenate([ct, key.encrypt(np.array([bad]), r[:1])])
+        with pytest.raises(ValueError, match="range check failed.*BitCount\\(\\)=21, expected 20"):
+            key.decrypt_in_range(ct2, 20)
+    big = key.encrypt_bn([pk.n_half], r[:1])
+    with pytest.raises(ValueError, match="range check failed"):
+        key.decrypt_in_range(big, 63)
+    with pytest.raises(ValueError, match="range check failed"):
+        key.decrypt_in_range(big, 500)
+    assert key.decrypt_in_range(big, pk.n_half.bit_length()) == [pk.n_half]
