@@ -280,3 +280,55 @@ class Key:
         out = np.empty((M, N, self.ct_limbs), dtype=np.uint32)
         capi.check(self.lib.hg_matmul(self.ctx.handle, self.id, _ptr(x), M, K, _ptr(y), N, _ptr(out)))
         return out
+
+    def select_sum(self, x, rows, cols=None):
+        """numpy Evaluator::SelectSum (numpy/evaluator.h:57-70) behind the pylib
+        select_sum extension (pylib/numpy_binding/extension_functions.cc:28-58):
+        the Sum of x[rows] (x of shape (n, S)) or x[rows][:, cols] (x of shape
+        (n, m, S)); `rows`/`cols` are anything NumPy indexes with (int arrays,
+        lists, slices, masks).  An empty tensor is an error; an empty selection
+        gives the ciphertext Sub(x[0], x[0]), the identity."""
+        x = np.ascontiguousarray(x, dtype=np.uint32)
+        if x.size == 0:
+            raise ValueError(f"you cannot select sum an empty tensor, shape={x.shape[:-1]}")
+        if x.ndim == 2:
+            if cols is not None:
+                raise ValueError("too many indices for array")
+            sub = x[rows]
+        else:
+            sub = x[rows][:, cols] if cols is not None else x[rows]
+        sub = sub.reshape(-1, self.ct_limbs)
+        if sub.shape[0] == 0:
+            return self._identity()
+        return self.sum(sub)
+
+    def batch_select_sum(self, x, selections):
+        """pylib batch_select_sum (extension_functions.cc:60-78): one Sum per row
+        selection, as (len(selections), S).  All selections of a group of up to
+        256 run as one bucket-sum launch (bucket = selection number) instead
+        of one reduction each."""
+        x = np.ascontiguousarray(x, dtype=np.uint32)
+        if x.size == 0:
+            raise ValueError(f"you cannot select sum an empty tensor, shape={x.shape[:-1]}")
+        flat = x.reshape(x.shape[0], -1, self.ct_limbs)
+        out = np.empty((len(selections), self.ct_limbs), dtype=np.uint32)
+        for g0 in range(0, len(selections), 256):
+            group = selections[g0:g0 + 256]
+            parts, ids = [], []
+            for b, sel in enumerate(group):
+                sub = flat[sel].reshape(-1, self.ct_limbs)
+                parts.append(sub)
+                ids.append(np.full(sub.shape[0], b, dtype=np.uint8))
+            if sum(p.shape[0] for p in parts) == 0:
+                out[g0:g0 + len(group)] = self._identity()
+                continue
+            xs = np.concatenate(parts, axis=0)
+            om = np.concatenate(ids).reshape(-1, 1)
+            res = self.bucket_sum(xs, om, len(group))
+            out[g0:g0 + len(group)] = res.reshape(len(group), self.ct_limbs)
+        return out
+
+    def _identity(self):
+        """Montgomery form of 1: Sub(c, c) for any valid c (evaluator.h:84-87)."""
+        r = np.zeros((1, self.r_limbs), dtype=np.uint32)
+        return self.encrypt(np.zeros(1, dtype=np.int64), r)

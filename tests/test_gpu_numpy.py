@@ -157,3 +157,35 @@ def test_decrypt_in_range(gpu_key):
     with pytest.raises(ValueError, match="range check failed"):
         key.decrypt_in_range(big, 500)
     assert key.decrypt_in_range(big, pk.n_half.bit_length()) == [pk.n_half]
+
+
+def test_select_sum_and_batch_select_sum(gpu_key):
+    """select_sum / batch_select_sum (numpy/evaluator.h:57-70,
+    extension_functions.cc:28-78) against the oracle's Sum of the selection;
+    an empty selection equals the engine's own Sub(x00, x00)."""
+    key, pk, sk = gpu_key(1024, 1)
+    rng = np.random.default_rng(9)
+    rows, cols = 40, 3
+    vals = rng.integers(-10 ** 6, 10 ** 6, size=(rows, cols))
+    ct, zs = enc_matrix(key, pk, vals, 61)
+    x = ct.reshape(rows, cols, -1)
+    sel = [3, 7, 7, 39]
+    got = key.select_sum(x, sel, [0, 2])
+    want = pz.sum_(pk, [zs[r * cols + c] for r in sel for c in (0, 2)])
+    assert zform(key, got) == [want]
+    x1 = x[:, 1]
+    got = key.select_sum(x1, slice(5, 25, 2))
+    assert zform(key, got) == [pz.sum_(pk, [zs[r * cols + 1] for r in range(5, 25, 2)])]
+    zero = key.select_sum(x1, [])
+    assert np.array_equal(zero, key.sub(x1[:1], x1[:1]))
+    with pytest.raises(ValueError):
+        key.select_sum(x1[:0], [])
+    sels = [list(rng.integers(0, rows, size=int(rng.integers(0, 6)))) for _ in range(300)]
+    sels[5] = []
+    outs = key.batch_select_sum(x1, sels)
+    assert outs.shape == (300, key.ct_limbs)
+    for i in (0, 5, 17, 255, 256, 299):
+        want = pz.sum_(pk, [zs[r * cols + 1] for r in sels[i]]) if sels[i] else 1
+        assert zform(key, outs[i:i + 1]) == [want], i
+    dec, _ = key.decrypt(outs)
+    assert dec.tolist() == [int(sum(vals[r, 1] for r in s)) for s in sels]
