@@ -228,7 +228,14 @@ def ours_arm(args):
     ctx = hg.Context(local)
     key = ctx.load_key(KEY_BITS, kp["n"], kp["h_s"], kp["p"], kp["q"], table_window=args.window)
     tuned = None
-    if not args.no_tune:
+    if args.key_config:
+        from heu_gb300 import autotune
+
+        cfg = autotune.get_config(key)
+        cfg.update({k: int(v) for k, v in (kv.split("=") for kv in args.key_config.split(","))})
+        autotune.set_config(key, cfg)
+        tuned = autotune.get_config(key)
+    elif not args.no_tune:
         from heu_gb300 import autotune
 
         tuned, _ = autotune.tune(key, calib=131072)
@@ -717,7 +724,8 @@ def c5_arm(args):
     def P(t):
         return ctypes.c_void_p(t.data_ptr())
 
-    server = hg.Server(ctx, budget_bytes=40 << 30, slots=4, max_batch_elems=1 << 18)
+    server = hg.Server(ctx, budget_bytes=40 << 30, slots=args.slots, max_batch_elems=1 << 18,
+                       batch_us=args.batch_us, slice_us=args.slice_us, policy=args.policy)
     for key in keys:
         m = torch.randint(-(2 ** 40), 2 ** 40, (LMAX,), dtype=torch.int64, device=dev, generator=gen)
         r = torch.randint(-(2 ** 31), 2 ** 31, (LMAX, key.r_limbs), dtype=torch.int32, device=dev, generator=gen)
@@ -764,9 +772,13 @@ def c5_arm(args):
         if seed == 1:
             continue
         nb = server.stats()["batches"] - b0
+        short = lens <= 1024
         results.append({"rate_req_per_s": rate, "requests": nreq,
                         "p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
                         "mean_ms": float(lat.mean() * 1e3),
+                        "short_le_1024": {"requests": int(short.sum()),
+                                          "p50_ms": float(np.percentile(lat[short], 50) * 1e3) if short.any() else None,
+                                          "p99_ms": float(np.percentile(lat[short], 99) * 1e3) if short.any() else None},
                         "throughput_req_per_s": nreq / wall.value,
                         "throughput_ops_per_s": float(lens.sum()) / wall.value,
                         "micro_batches": int(nb), "wall_s": wall.value})
@@ -815,7 +827,9 @@ def c5_arm(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
         "config": {"workload": "config5", "keys": "6x2048 + 2x3072 resident", "len": [1, LMAX],
                    "op_mix": dict(zip(["encrypt", "add", "mul", "sum", "decrypt"], weights)),
-                   "budget_bytes": 40 << 30, "slots": 4, "max_batch_elems": 1 << 18},
+                   "budget_bytes": 40 << 30, "slots": args.slots, "max_batch_elems": 1 << 18,
+                   "batch_us": args.batch_us or 100000.0, "slice_us": args.slice_us or 50000.0,
+                   "policy": ["shortest-remaining-first", "fifo"][args.policy]},
         "rates": results,
         "plain_per_call_ops_per_s": plain_ops,
         "served_over_plain": peak_served / plain_ops,
@@ -839,7 +853,14 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", choices=["config2", "config3", "config4", "config5"], default="config2")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner")
+    ap.add_argument("--key-config", default=None,
+                    help="explicit key config instead of the autotuner, e.g. "
+                         "'variant=0,dec_variant=0,mul_window=3,dec_window=6' (profiling a fixed kernel)")
     ap.add_argument("--quick", action="store_true", help="config5: two arrival rates only")
+    ap.add_argument("--batch-us", type=float, default=0.0, help="config5: server micro-batch target (0 = default)")
+    ap.add_argument("--slice-us", type=float, default=0.0, help="config5: server slice per request (0 = default)")
+    ap.add_argument("--slots", type=int, default=4, help="config5: concurrent micro-batches")
+    ap.add_argument("--policy", type=int, default=0, choices=[0, 1], help="config5: 0 shortest-first, 1 fifo")
     ap.add_argument("--ops", default="encrypt,add,mul,decrypt",
                     help="subset of the step's ops (for profiling one kernel)")
     args = ap.parse_args()

@@ -105,7 +105,8 @@ class ServerConfig(ctypes.Structure):
     """hg_server_config"""
 
     _fields_ = [("budget_bytes", ctypes.c_size_t), ("slots", ctypes.c_int), ("max_batch_elems", ctypes.c_size_t),
-                ("variant", ctypes.c_int), ("batch_us", ctypes.c_double), ("slice_us", ctypes.c_double)]
+                ("variant", ctypes.c_int), ("batch_us", ctypes.c_double), ("slice_us", ctypes.c_double),
+                ("policy", ctypes.c_int)]
 
 
 class Request(ctypes.Structure):

@@ -1674,6 +1674,8 @@ int hg_server_create(hg_ctx* ctx, const hg_server_config* cfg, hg_server** out) 
     s->variant = c.variant;
     if (cfg && cfg->batch_us > 0) s->batch_us = cfg->batch_us;
     if (cfg && cfg->slice_us > 0) s->slice_us = cfg->slice_us;
+    if (cfg && (cfg->policy < 0 || cfg->policy > 1)) fail(HG_ERR_INVALID, "policy must be 0 or 1");
+    s->policy = cfg ? cfg->policy : 0;
     // batch-kernel scratch: the largest per-warp table over the loaded keys
     size_t warp_words = 1;
     {

@@ -114,6 +114,7 @@ struct hg_server {
   int variant = 0;
   double batch_us = 100000.0;  // target GPU time of one micro-batch
   double slice_us = 50000.0;   // most GPU time one request gets per micro-batch
+  int policy = 0;              // HG_POLICY_SHORTEST or HG_POLICY_FIFO
   std::thread sched;
 };
 
@@ -311,7 +312,15 @@ void scheduler(hg_server* sp) {
       if (!any) break;
     }
     // admit: every pending request gets a slice of at most slice_us of work
-    // per micro-batch (processor sharing), until the batch reaches batch_us
+    // per micro-batch (processor sharing), until the batch reaches batch_us;
+    // with HG_POLICY_SHORTEST the requests with the least estimated remaining
+    // work are offered first, so short requests do not queue behind long ones
+    if (s.policy == HG_POLICY_SHORTEST && s.pending.size() > 1)
+      std::stable_sort(s.pending.begin(), s.pending.end(), [](const Req* a, const Req* b) {
+        const double ra = elem_cost_us(*a->k, a->r.op) * (double)(a->r.count - a->next);
+        const double rb = elem_cost_us(*b->k, b->r.op) * (double)(b->r.count - b->next);
+        return ra < rb;
+      });
     bool launched = false;
     for (auto& slp : s.slots) {
       Slot& sl = *slp;

@@ -202,7 +202,13 @@ typedef struct {
                              micro-batch (0 = 50000); longer requests are cut
                              into slices so short ones are not stuck behind
                              them (sums are never cut) */
+  int policy;             /* admission order: HG_POLICY_SHORTEST (0, pending
+                             requests with the least estimated remaining work
+                             first, arrival order among equals) or
+                             HG_POLICY_FIFO (1, arrival order) */
 } hg_server_config;
+#define HG_POLICY_SHORTEST 0
+#define HG_POLICY_FIFO 1
 typedef struct {
   int key_id;
   int op;           /* HG_OP_ENCRYPT / DECRYPT / ADD / MUL / SUM */

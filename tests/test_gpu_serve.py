@@ -27,10 +27,11 @@ def _alone(key, op, x0, x1):
     return key.sum(x0)
 
 
-def test_served_results_equal_alone(gpu_ctx, gpu_key):
+@pytest.mark.parametrize("policy", [hg.Server.SHORTEST, hg.Server.FIFO])
+def test_served_results_equal_alone(gpu_ctx, gpu_key, policy):
     keys = [gpu_key(2048, 0)[0], gpu_key(3072, 2)[0], gpu_key(1024, 1)[0]]
     rng = np.random.default_rng(17)
-    server = hg.Server(gpu_ctx, budget_bytes=2 << 30, slots=3, max_batch_elems=1 << 14)
+    server = hg.Server(gpu_ctx, budget_bytes=2 << 30, slots=3, max_batch_elems=1 << 14, policy=policy)
     # one resident vector per key
     vec_len = 3000
     residents, res_host = [], []
