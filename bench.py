@@ -649,10 +649,11 @@ def c3_arm(args):
         capi.check(lib.hg_dev_matmul(h, key.id, P(ct), M, K, ctypes.c_void_p(yc.ctypes.data), N, P(mm), sp))
 
     res = {}
-    for name, fn, units, macs_per_unit in (
-            ("sum", run_sum, n, mm_macs(128)),
-            ("bucket_sum", run_bucket, n * F, mm_macs(128)),
-            ("matmul", run_matmul, M * N, (K + 16) * mm_macs(128))):
+    cb = key.ct_limbs * 4
+    for name, fn, units, macs_per_unit, nbytes in (
+            ("sum", run_sum, n, mm_macs(128), n * cb + cb),
+            ("bucket_sum", run_bucket, n * F, mm_macs(128), n * cb + n * F + F * B * cb),
+            ("matmul", run_matmul, M * N, (K + 16) * mm_macs(128), M * K * cb + K * N * 8 + M * N * cb)):
         for _ in range(max(1, args.warmup)):
             fn()
         torch.cuda.synchronize()
@@ -665,7 +666,8 @@ def c3_arm(args):
             e1.record(stream)
         torch.cuda.synchronize()
         dt = e0.elapsed_time(e1) / 1e3 / args.steps
-        res[name] = {"seconds": dt, "units_per_s": units / dt, "algorithmic_tmacs": units * macs_per_unit / dt / 1e12}
+        res[name] = {"seconds": dt, "units_per_s": units / dt, "algorithmic_tmacs": units * macs_per_unit / dt / 1e12,
+                     "algorithmic_bytes": nbytes, "hbm_gbs": nbytes / dt / 1e9}
     capi.check(lib.hg_dev_check(h))
     # correctness through decryption
     key_dec = lambda t: key.decrypt(t.cpu().numpy().view(np.uint32))  # noqa: E731
@@ -743,6 +745,8 @@ def c5_arm(args):
     hnd = (ctypes.c_uint64 * len(keys))(*handles)
     weights = [0.30, 0.20, 0.25, 0.15, 0.10]  # encrypt, add, mul, sum, decrypt
     rates = [100, 300, 1000, 3000, 10000, 50000] if not args.quick else [300, 3000]
+    if args.rates:
+        rates = [int(v) for v in args.rates.split(",")]
     results = []
     # warm-up: a short stream
     for rate, nreq, seed in [(1000, 50, 1)] + [(rt, 0, 0) for rt in rates]:
@@ -861,6 +865,7 @@ def main():
     ap.add_argument("--slice-us", type=float, default=0.0, help="config5: server slice per request (0 = default)")
     ap.add_argument("--slots", type=int, default=4, help="config5: concurrent micro-batches")
     ap.add_argument("--policy", type=int, default=0, choices=[0, 1], help="config5: 0 shortest-first, 1 fifo")
+    ap.add_argument("--rates", default="", help="config5: comma-separated arrival rates (req/s)")
     ap.add_argument("--ops", default="encrypt,add,mul,decrypt",
                     help="subset of the step's ops (for profiling one kernel)")
     args = ap.parse_args()

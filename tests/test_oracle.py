@@ -205,6 +205,33 @@ def test_golden_fixtures_reproduce():
         assert [int(v, 16) for v in c["mul"]] == [pz.mul(pk, z, k) for z, k in zip(zs, ks)]
         assert int(c["sum"], 16) == pz.sum_(pk, zs)
         assert [int(v, 16) for v in c["negate"]] == [pz.negate(pk, z) for z in zs]
+        nz = len(zs)
+        assert [int(v, 16) for v in c["sub_next"]] == [pz.sub(pk, zs[i], zs[(i + 1) % nz]) for i in range(nz)]
+        km = [int(v) for v in c["k_more"]]
+        assert [int(v, 16) for v in c["mul_more"]] == [pz.mul(pk, zs[i], k) for i, k in enumerate(km)]
+        big = [int(v) for v in c["m_big"]]
+        assert big[0] == pk.n_half - 1 and big[2] == pk.n_half
+        zb = [pz.encrypt(pk, m, int(r, 16)) for m, r in zip(big, c["r_big"])]
+        assert [int(v, 16) for v in c["ct_big_z"]] == zb
+        assert [pz.decrypt(pk, sk, z) for z in zb] == big
+        if "sum_0_899" in c:
+            e = c["sum_0_899"]
+            rs9 = pz.r_stream(e["r_seed"], 900, pk.key_size // 2)
+            s9 = pz.sum_(pk, [pz.encrypt(pk, m, r) for m, r in zip(range(900), rs9)])
+            assert int(e["ct_z"], 16) == s9 and pz.decrypt(pk, sk, s9) == 404550
+            b = c["bucket_sum"]
+            rr = pz.r_stream(b["r_seed"], 24, pk.key_size // 2)
+            xz = [[pz.encrypt(pk, b["vals"][i][col], rr[2 * i + col]) for col in range(2)] for i in range(12)]
+            for key, cs in (("out_z", False), ("out_cumsum_z", True)):
+                got = pz.bucket_sum(pk, xz, b["order_map"], b["buckets"], cumsum=cs)
+                assert [[int(v, 16) for v in row] for row in b[key]] == got
+            mm = c["matmul"]
+            rm = pz.r_stream(mm["r_seed"], 12, pk.key_size // 2)
+            xmz = [[pz.encrypt(pk, mm["x"][i][j], rm[4 * i + j]) for j in range(4)] for i in range(3)]
+            out = pz.matmul(pk, xmz, mm["y"])
+            assert [[int(v, 16) for v in row] for row in mm["out_z"]] == out
+            want = [[sum(mm["x"][i][k] * mm["y"][k][j] for k in range(4)) for j in range(2)] for i in range(3)]
+            assert [[pz.decrypt(pk, sk, v) for v in row] for row in out] == want
 
 
 @pytest.mark.parametrize("bits,seed", [(1024, 1), (2048, 0)])
