@@ -416,6 +416,31 @@ def ours_arm(args):
                "d2h_bytes_per_step": d2h, "steps": args.e2e_steps,
                "api": "hg_encrypt/hg_add/hg_mul/hg_decrypt (host pointers, pinned)"}
 
+    # per-call latency of small host-pointer calls (no per-call allocation:
+    # staging buffers and streams belong to the context)
+    small = {}
+    if not args.no_e2e:
+        for cnt in (1, 16, 256, 4096):
+            mh = m[:cnt].cpu().numpy()
+            rh = r[:cnt].cpu().numpy().view(np.uint32)
+            cth = np.empty((cnt, S), np.uint32)
+            dh = np.empty(cnt, np.int64)
+            oh = np.empty(cnt, np.uint8)
+            ts = {"encrypt": [], "decrypt": []}
+            for it in range(12):
+                t = time.perf_counter()
+                capi.check(lib.hg_encrypt(h, key.id, ctypes.c_void_p(mh.ctypes.data), ctypes.c_void_p(rh.ctypes.data),
+                                          ctypes.c_void_p(cth.ctypes.data), cnt))
+                t2 = time.perf_counter()
+                capi.check(lib.hg_decrypt(h, key.id, ctypes.c_void_p(cth.ctypes.data), ctypes.c_void_p(dh.ctypes.data),
+                                          ctypes.c_void_p(oh.ctypes.data), cnt))
+                t3 = time.perf_counter()
+                if it >= 2:
+                    ts["encrypt"].append((t2 - t) * 1e6)
+                    ts["decrypt"].append((t3 - t2) * 1e6)
+            assert np.array_equal(dh, mh), "small-call decrypt mismatch"
+            small[str(cnt)] = {k: float(np.median(v)) for k, v in ts.items()}
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         rates, step_rate, cores, sample = cpu_sample()
@@ -439,6 +464,7 @@ def ours_arm(args):
                          "peak_chain_pattern": peak_chain, "peak_wide_pattern": peak_wide,
                          "per_op_tmacs": roof_ops},
             "e2e": e2e,
+            "small_call_us": small,
             "cpu_baseline": cpu,
             "gpu_launches": launches,
             "clocks": clocks,
