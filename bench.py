@@ -753,7 +753,8 @@ def c5_arm(args):
         return ctypes.c_void_p(t.data_ptr())
 
     server = hg.Server(ctx, budget_bytes=40 << 30, slots=args.slots, max_batch_elems=1 << 18,
-                       batch_us=args.batch_us, slice_us=args.slice_us, policy=args.policy)
+                       batch_us=args.batch_us, slice_us=args.slice_us, policy=args.policy,
+                       express_us=args.express_us)
     for key in keys:
         m = torch.randint(-(2 ** 40), 2 ** 40, (LMAX,), dtype=torch.int64, device=dev, generator=gen)
         r = torch.randint(-(2 ** 31), 2 ** 31, (LMAX, key.r_limbs), dtype=torch.int32, device=dev, generator=gen)
@@ -859,7 +860,8 @@ def c5_arm(args):
                    "op_mix": dict(zip(["encrypt", "add", "mul", "sum", "decrypt"], weights)),
                    "budget_bytes": 40 << 30, "slots": args.slots, "max_batch_elems": 1 << 18,
                    "batch_us": args.batch_us or 100000.0, "slice_us": args.slice_us or 50000.0,
-                   "policy": ["shortest-remaining-first", "fifo"][args.policy]},
+                   "policy": ["shortest-remaining-first", "fifo"][args.policy],
+                   "express_us": args.express_us or 2000.0},
         "rates": results,
         "plain_per_call_ops_per_s": plain_ops,
         "served_over_plain": peak_served / plain_ops,
@@ -892,6 +894,8 @@ def main():
     ap.add_argument("--slots", type=int, default=4, help="config5: concurrent micro-batches")
     ap.add_argument("--policy", type=int, default=0, choices=[0, 1], help="config5: 0 shortest-first, 1 fifo")
     ap.add_argument("--rates", default="", help="config5: comma-separated arrival rates (req/s)")
+    ap.add_argument("--express-us", type=float, default=0.0,
+                    help="config5: express-slot threshold in estimated GPU us (0 = default, < 0 = off)")
     ap.add_argument("--ops", default="encrypt,add,mul,decrypt",
                     help="subset of the step's ops (for profiling one kernel)")
     args = ap.parse_args()

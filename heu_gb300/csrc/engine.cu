@@ -1676,6 +1676,13 @@ int hg_server_create(hg_ctx* ctx, const hg_server_config* cfg, hg_server** out) 
     if (cfg && cfg->slice_us > 0) s->slice_us = cfg->slice_us;
     if (cfg && (cfg->policy < 0 || cfg->policy > 1)) fail(HG_ERR_INVALID, "policy must be 0 or 1");
     s->policy = cfg ? cfg->policy : 0;
+    const int resident = hg::batch_resident_blocks(c.variant);
+    s->express_us = (cfg && cfg->express_us != 0.0) ? cfg->express_us : 2000.0;
+    double share = (cfg && cfg->express_share > 0.0) ? cfg->express_share : 0.125;
+    if (share >= 1.0) fail(HG_ERR_INVALID, "express_share must be below 1");
+    if (c.slots < 2) s->express_us = -1.0;
+    s->express_grid = std::max(1, (int)(resident * share + 0.5));
+    s->regular_grid = s->express_us >= 0.0 ? std::max(1, resident - s->express_grid) : resident;
     // batch-kernel scratch: the largest per-warp table over the loaded keys
     size_t warp_words = 1;
     {
@@ -1692,8 +1699,13 @@ int hg_server_create(hg_ctx* ctx, const hg_server_config* cfg, hg_server** out) 
     const size_t arena = c.budget_bytes / (size_t)c.slots;
     for (int i = 0; i < c.slots; ++i) {
       auto sl = std::make_unique<Slot>();
-      cuda_check(cudaStreamCreateWithFlags(&sl->st, cudaStreamNonBlocking), "stream");
+      sl->express = (i == 0 && s->express_us >= 0.0);
+      int lo_prio = 0, hi_prio = 0;
+      cuda_check(cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio), "priority range");
+      cuda_check(cudaStreamCreateWithPriority(&sl->st, cudaStreamNonBlocking, sl->express ? hi_prio : lo_prio),
+                 "stream");
       cuda_check(cudaEventCreateWithFlags(&sl->ev, cudaEventDisableTiming), "event");
+      cuda_check(cudaEventCreateWithFlags(&sl->kev, cudaEventDisableTiming), "event");
       sl->dev.base = sl->dev_mem.ensure<uint8_t>(arena);
       sl->dev.cap = arena;
       sl->pin.base = sl->pin_mem.ensure<uint8_t>((size_t)16 << 20);
@@ -1724,6 +1736,7 @@ int hg_server_destroy(hg_server* s) {
       cudaStreamSynchronize(sl->st);
       cudaStreamDestroy(sl->st);
       cudaEventDestroy(sl->ev);
+      cudaEventDestroy(sl->kev);
     }
     delete s;
     return HG_OK;

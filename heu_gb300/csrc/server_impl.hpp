@@ -74,6 +74,8 @@ struct Slot {
   size_t bytes = 0;
   uint32_t* err_host = nullptr;
   bool busy = false;
+  bool express = false;      // runs short requests on a reserved share of the GPU
+  cudaEvent_t kev = nullptr; // recorded after this slot's batch kernel
 };
 
 size_t slice_dev_bytes(const KeyRec& k, const hg_request& r, size_t n) {
@@ -115,6 +117,10 @@ struct hg_server {
   double batch_us = 100000.0;  // target GPU time of one micro-batch
   double slice_us = 50000.0;   // most GPU time one request gets per micro-batch
   int policy = 0;              // HG_POLICY_SHORTEST or HG_POLICY_FIFO
+  double express_us = -1.0;    // short-request threshold of the express slot (< 0: none)
+  int express_grid = 0;        // batch-kernel blocks of the express slot
+  int regular_grid = 0;        // batch-kernel blocks of every other slot
+  cudaEvent_t last_kernel = nullptr;  // kernel-done event of the latest regular batch
   std::thread sched;
 };
 
@@ -234,12 +240,20 @@ void run_slot(hg_server& s, Slot& sl) {
     cuda_check(cudaMemcpyAsync(dj, hj, jb, cudaMemcpyHostToDevice, st), "H2D jobs");
     cuda_check(cudaMemcpyAsync(dt, ht, tb, cudaMemcpyHostToDevice, st), "H2D tiles");
     cuda_check(cudaMemsetAsync(sl.counter.p, 0, 4, st), "memset counter");
-    const int grid = hg::batch_resident_blocks(s.variant);
+    const int grid = sl.express ? s.express_grid : s.regular_grid;
     if ((size_t)grid * hg::batch_warps_per_block() * plan.warp_words * 4 > sl.scratch.n)
       fail(HG_ERR_NOMEM, "server scratch too small for this batch");
+    // with an express slot, regular batch kernels run one after another on
+    // their share of the blocks, so the express share stays free
+    if (!sl.express && s.express_us >= 0.0 && s.last_kernel)
+      cuda_check(cudaStreamWaitEvent(st, s.last_kernel, 0), "wait previous batch");
     cuda_check(hg::launch_batch(s.variant, dj, dt, (uint32_t)plan.tiles.size(), sl.counter.as<uint32_t>(),
                                 sl.scratch.as<uint32_t>(), plan.warp_words, err, grid, st),
                "batch launch");
+    if (!sl.express && s.express_us >= 0.0) {
+      cuda_check(cudaEventRecord(sl.kev, st), "event");
+      s.last_kernel = sl.kev;
+    }
   }
   for (auto& iv : invs) {
     iv.task->status = 0;
@@ -322,13 +336,31 @@ void scheduler(hg_server* sp) {
         return ra < rb;
       });
     bool launched = false;
+    // short requests (estimated remaining work <= express_us) belong to the
+    // express slot unless their backlog exceeds what it takes per batch
+    double short_backlog = 0.0;
+    if (s.express_us >= 0.0)
+      for (const Req* q : s.pending) {
+        const double rem = elem_cost_us(*q->k, q->r.op) * (double)(q->r.count - q->next);
+        if (rem <= s.express_us) short_backlog += rem;
+      }
+    const double express_batch_us = 4.0 * std::max(s.express_us, 1.0);
     for (auto& slp : s.slots) {
       Slot& sl = *slp;
       if (sl.busy || s.pending.empty()) continue;
       size_t elems = 0, bytes = 0;
       double cost = 0.0;
+      const double batch_cap = sl.express ? express_batch_us : s.batch_us;
       for (auto it = s.pending.begin(); it != s.pending.end();) {
         Req* q = *it;
+        if (s.express_us >= 0.0) {
+          const double rem = elem_cost_us(*q->k, q->r.op) * (double)(q->r.count - q->next);
+          const bool is_short = rem <= s.express_us;
+          if ((sl.express && !is_short) || (!sl.express && is_short && short_backlog <= express_batch_us)) {
+            ++it;
+            continue;
+          }
+        }
         if (q->next == 0 && q->outstanding == 0 && !q->p0 && !q->p1 && (q->r.h0 || q->r.h1)) {
           try {
             q->p0 = q->r.h0 ? resident_ptr(s, q->r.h0, *q->k, q->r.count) : nullptr;
@@ -352,7 +384,7 @@ void scheduler(hg_server* sp) {
         const size_t need = slice_dev_bytes(*q->k, q->r, len);
         const bool first = sl.slices.empty();
         if (!first && (elems + len > s.cfg.max_batch_elems || bytes + need > sl.dev.cap ||
-                       s.inflight + bytes + need > s.cfg.budget_bytes || cost >= s.batch_us))
+                       s.inflight + bytes + need > s.cfg.budget_bytes || cost >= batch_cap))
           break;
         if (first && s.inflight + need > s.cfg.budget_bytes && s.inflight > 0) break;  // wait for memory
         std::unique_ptr<InvTask> task;

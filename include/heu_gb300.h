@@ -206,6 +206,13 @@ typedef struct {
                              requests with the least estimated remaining work
                              first, arrival order among equals) or
                              HG_POLICY_FIFO (1, arrival order) */
+  double express_us;      /* requests with at most this much estimated GPU
+                             work run in an express slot that keeps a share of
+                             every SM free for them, so they do not wait for
+                             long batches (0 = 2000; < 0 = no express slot;
+                             needs slots >= 2) */
+  double express_share;   /* share of the batch kernel's resident blocks kept
+                             for the express slot (0 = 0.125) */
 } hg_server_config;
 #define HG_POLICY_SHORTEST 0
 #define HG_POLICY_FIFO 1

@@ -90,11 +90,14 @@ def test_served_results_equal_alone(gpu_ctx, gpu_key, policy):
     server.close()
 
 
-def test_long_requests_are_sliced_and_stay_exact(gpu_ctx, gpu_key):
+@pytest.mark.parametrize("express_us", [0.0, -1.0], ids=["express", "no-express"])
+def test_long_requests_are_sliced_and_stay_exact(gpu_ctx, gpu_key, express_us):
     """Requests far longer than one slice (tiny slice budget) still give the
-    per-call result, interleaved with short ones."""
+    per-call result, interleaved with short ones, with and without the
+    express slot (which takes the 3-element request here)."""
     key, pk, sk = gpu_key(2048, 0)
-    server = hg.Server(gpu_ctx, budget_bytes=1 << 30, slots=2, slice_us=50.0, batch_us=400.0)
+    server = hg.Server(gpu_ctx, budget_bytes=1 << 30, slots=2, slice_us=50.0, batch_us=400.0,
+                       express_us=express_us)
     rng = np.random.default_rng(23)
     n = 5000
     m = rng.integers(-(2 ** 40), 2 ** 40, size=n)
