@@ -861,7 +861,7 @@ def c5_arm(args):
                    "budget_bytes": 40 << 30, "slots": args.slots, "max_batch_elems": 1 << 18,
                    "batch_us": args.batch_us or 100000.0, "slice_us": args.slice_us or 50000.0,
                    "policy": ["shortest-remaining-first", "fifo"][args.policy],
-                   "express_us": args.express_us or 2000.0},
+                   "express_us": args.express_us if args.express_us > 0 else None},
         "rates": results,
         "plain_per_call_ops_per_s": plain_ops,
         "served_over_plain": peak_served / plain_ops,
@@ -895,7 +895,7 @@ def main():
     ap.add_argument("--policy", type=int, default=0, choices=[0, 1], help="config5: 0 shortest-first, 1 fifo")
     ap.add_argument("--rates", default="", help="config5: comma-separated arrival rates (req/s)")
     ap.add_argument("--express-us", type=float, default=0.0,
-                    help="config5: express-slot threshold in estimated GPU us (0 = default, < 0 = off)")
+                    help="config5: express-slot threshold in estimated GPU us (0 = no express slot)")
     ap.add_argument("--ops", default="encrypt,add,mul,decrypt",
                     help="subset of the step's ops (for profiling one kernel)")
     args = ap.parse_args()

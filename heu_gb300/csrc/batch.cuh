@@ -45,6 +45,12 @@ int batch_resident_blocks(int variant);
 int batch_warps_per_block();
 cudaError_t launch_batch(int variant, const BatchJob* jobs, const BatchTile* tiles, uint32_t ntiles,
                          uint32_t* counter, uint32_t* scratch, size_t warp_words, uint32_t* err, int grid,
-                         cudaStream_t st);
+                         cudaStream_t st, size_t dyn_smem = 0);
+// Resident blocks per SM of the batch kernel (register-limited).
+int batch_blocks_per_sm(int variant);
+// Dynamic shared memory that limits the batch kernel to `blocks_per_sm`
+// resident blocks per SM (sets the kernel's shared-memory attributes); the
+// blocks it keeps free run another launch of the kernel without padding.
+size_t batch_smem_cap(int variant, int blocks_per_sm);
 
 }  // namespace hg

@@ -119,14 +119,43 @@ int batch_warps_per_block() { return kWarps; }
 
 cudaError_t launch_batch(int variant, const BatchJob* jobs, const BatchTile* tiles, uint32_t ntiles,
                          uint32_t* counter, uint32_t* scratch, size_t warp_words, uint32_t* err, int grid,
-                         cudaStream_t st) {
+                         cudaStream_t st, size_t dyn_smem) {
   if (ntiles == 0) return cudaSuccess;
   if (variant)
-    k_batch<1><<<grid, kBlock, 0, st>>>(jobs, tiles, ntiles, counter, scratch, warp_words, err);
+    k_batch<1><<<grid, kBlock, dyn_smem, st>>>(jobs, tiles, ntiles, counter, scratch, warp_words, err);
   else
-    k_batch<0><<<grid, kBlock, 0, st>>>(jobs, tiles, ntiles, counter, scratch, warp_words, err);
+    k_batch<0><<<grid, kBlock, dyn_smem, st>>>(jobs, tiles, ntiles, counter, scratch, warp_words, err);
   count_launches(1);
   return cudaGetLastError();
+}
+
+template <typename K>
+static size_t smem_cap_pad(K kernel, int cap) {
+  int dev = 0, per_sm = 0, reserved = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+  cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+  cudaFuncAttributes fa{};
+  cudaFuncGetAttributes(&fa, kernel);
+  // cap blocks fit in per_sm, cap + 1 do not
+  const size_t per_block = (size_t)((double)per_sm / ((double)cap + 0.5));
+  const size_t used = fa.sharedSizeBytes + (size_t)reserved;
+  const size_t pad = per_block > used ? per_block - used : 0;
+  cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pad);
+  return pad;
+}
+
+size_t batch_smem_cap(int variant, int blocks_per_sm) {
+  if (blocks_per_sm < 1) blocks_per_sm = 1;
+  return variant ? smem_cap_pad(k_batch<1>, blocks_per_sm) : smem_cap_pad(k_batch<0>, blocks_per_sm);
+}
+
+int batch_blocks_per_sm(int variant) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return batch_resident_blocks(variant) / (sms > 0 ? sms : 1);
 }
 
 }  // namespace hg

@@ -1677,12 +1677,20 @@ int hg_server_create(hg_ctx* ctx, const hg_server_config* cfg, hg_server** out) 
     if (cfg && (cfg->policy < 0 || cfg->policy > 1)) fail(HG_ERR_INVALID, "policy must be 0 or 1");
     s->policy = cfg ? cfg->policy : 0;
     const int resident = hg::batch_resident_blocks(c.variant);
-    s->express_us = (cfg && cfg->express_us != 0.0) ? cfg->express_us : 2000.0;
-    double share = (cfg && cfg->express_share > 0.0) ? cfg->express_share : 0.125;
+    const int bps = hg::batch_blocks_per_sm(c.variant);
+    const int sms = std::max(1, resident / std::max(1, bps));
+    s->express_us = (cfg && cfg->express_us != 0.0) ? cfg->express_us : -1.0;
+    const double share = (cfg && cfg->express_share > 0.0) ? cfg->express_share : 0.25;
     if (share >= 1.0) fail(HG_ERR_INVALID, "express_share must be below 1");
-    if (c.slots < 2) s->express_us = -1.0;
-    s->express_grid = std::max(1, (int)(resident * share + 0.5));
-    s->regular_grid = s->express_us >= 0.0 ? std::max(1, resident - s->express_grid) : resident;
+    if (c.slots < 2 || bps < 2) s->express_us = -1.0;
+    s->regular_grid = resident;
+    if (s->express_us >= 0.0) {
+      // express: `eb` blocks on every SM; regular batches: the rest
+      const int eb = std::min(bps - 1, std::max(1, (int)(share * bps + 0.5)));
+      s->express_grid = eb * sms;
+      s->regular_grid = (bps - eb) * sms;
+      s->regular_smem = hg::batch_smem_cap(c.variant, bps - eb);
+    }
     // batch-kernel scratch: the largest per-warp table over the loaded keys
     size_t warp_words = 1;
     {
@@ -1705,7 +1713,6 @@ int hg_server_create(hg_ctx* ctx, const hg_server_config* cfg, hg_server** out) 
       cuda_check(cudaStreamCreateWithPriority(&sl->st, cudaStreamNonBlocking, sl->express ? hi_prio : lo_prio),
                  "stream");
       cuda_check(cudaEventCreateWithFlags(&sl->ev, cudaEventDisableTiming), "event");
-      cuda_check(cudaEventCreateWithFlags(&sl->kev, cudaEventDisableTiming), "event");
       sl->dev.base = sl->dev_mem.ensure<uint8_t>(arena);
       sl->dev.cap = arena;
       sl->pin.base = sl->pin_mem.ensure<uint8_t>((size_t)16 << 20);
@@ -1736,7 +1743,6 @@ int hg_server_destroy(hg_server* s) {
       cudaStreamSynchronize(sl->st);
       cudaStreamDestroy(sl->st);
       cudaEventDestroy(sl->ev);
-      cudaEventDestroy(sl->kev);
     }
     delete s;
     return HG_OK;

@@ -74,8 +74,7 @@ struct Slot {
   size_t bytes = 0;
   uint32_t* err_host = nullptr;
   bool busy = false;
-  bool express = false;      // runs short requests on a reserved share of the GPU
-  cudaEvent_t kev = nullptr; // recorded after this slot's batch kernel
+  bool express = false;  // runs short requests on a reserved share of every SM
 };
 
 size_t slice_dev_bytes(const KeyRec& k, const hg_request& r, size_t n) {
@@ -120,7 +119,8 @@ struct hg_server {
   double express_us = -1.0;    // short-request threshold of the express slot (< 0: none)
   int express_grid = 0;        // batch-kernel blocks of the express slot
   int regular_grid = 0;        // batch-kernel blocks of every other slot
-  cudaEvent_t last_kernel = nullptr;  // kernel-done event of the latest regular batch
+  size_t regular_smem = 0;     // dynamic shared memory that keeps regular batches
+                               // off the express slot's blocks on every SM
   std::thread sched;
 };
 
@@ -243,17 +243,13 @@ void run_slot(hg_server& s, Slot& sl) {
     const int grid = sl.express ? s.express_grid : s.regular_grid;
     if ((size_t)grid * hg::batch_warps_per_block() * plan.warp_words * 4 > sl.scratch.n)
       fail(HG_ERR_NOMEM, "server scratch too small for this batch");
-    // with an express slot, regular batch kernels run one after another on
-    // their share of the blocks, so the express share stays free
-    if (!sl.express && s.express_us >= 0.0 && s.last_kernel)
-      cuda_check(cudaStreamWaitEvent(st, s.last_kernel, 0), "wait previous batch");
+    // regular batches carry shared-memory padding that caps them below the
+    // per-SM block limit, so however many overlap, every SM keeps room for
+    // the express slot's blocks
     cuda_check(hg::launch_batch(s.variant, dj, dt, (uint32_t)plan.tiles.size(), sl.counter.as<uint32_t>(),
-                                sl.scratch.as<uint32_t>(), plan.warp_words, err, grid, st),
+                                sl.scratch.as<uint32_t>(), plan.warp_words, err, grid, st,
+                                sl.express ? 0 : s.regular_smem),
                "batch launch");
-    if (!sl.express && s.express_us >= 0.0) {
-      cuda_check(cudaEventRecord(sl.kev, st), "event");
-      s.last_kernel = sl.kev;
-    }
   }
   for (auto& iv : invs) {
     iv.task->status = 0;

@@ -206,13 +206,14 @@ typedef struct {
                              requests with the least estimated remaining work
                              first, arrival order among equals) or
                              HG_POLICY_FIFO (1, arrival order) */
-  double express_us;      /* requests with at most this much estimated GPU
-                             work run in an express slot that keeps a share of
-                             every SM free for them, so they do not wait for
-                             long batches (0 = 2000; < 0 = no express slot;
-                             needs slots >= 2) */
-  double express_share;   /* share of the batch kernel's resident blocks kept
-                             for the express slot (0 = 0.125) */
+  double express_us;      /* > 0: requests with at most this much estimated
+                             GPU work run in an express slot (slot 0) that
+                             keeps a share of every SM's blocks free for them,
+                             so they do not wait for long batches; the other
+                             batches then run on the remaining share
+                             (0 or < 0 = no express slot; needs slots >= 2) */
+  double express_share;   /* share of every SM's batch-kernel blocks kept for
+                             the express slot (0 = 0.25, i.e. 1 of 4) */
 } hg_server_config;
 #define HG_POLICY_SHORTEST 0
 #define HG_POLICY_FIFO 1
