@@ -1,0 +1,340 @@
+"""heu.numpy-style tensors over the engine.
+
+Mirrors the Python surface of HEU's heu.numpy module for this schema
+(heu/pylib/numpy_binding/bind_numpy.cc:381-480, extension_functions.cc:28-138):
+``setup`` returns a kit with ``encryptor()``, ``decryptor()``, ``evaluator()``
+and ``array()``; the evaluator offers add / sub / mul (with NumPy broadcasting
+of the two shapes, numpy/evaluator.cc:160-185), matmul, sum, select_sum,
+batch_select_sum, feature_wise_bucket_sum and batch_feature_wise_bucket_sum.
+
+Plaintexts are integers (int64 NumPy arrays, or Python ints up to n/2 in an
+object array); HEU's encoders are not part of this path.  Ciphertexts are
+kept as a (size, S) uint32 limb array in Montgomery form with a logical
+shape, exactly the bytes the C-ABI exchanges.
+"""
+
+import os
+
+import numpy as np
+
+from heu_gb300 import engine
+
+_I64_MIN, _I64_MAX = -(2 ** 63), 2 ** 63 - 1
+
+
+def _as_values(values):
+    a = np.asarray(values, dtype=object) if not isinstance(values, np.ndarray) else values
+    if a.dtype != object:
+        return np.asarray(a, dtype=np.int64)
+    flat = [int(v) for v in a.reshape(-1)]
+    if all(_I64_MIN <= v <= _I64_MAX for v in flat):
+        return np.array(flat, dtype=np.int64).reshape(a.shape)
+    out = np.empty(len(flat), dtype=object)
+    out[:] = flat
+    return out.reshape(a.shape)
+
+
+class PlaintextArray:
+    """Integer tensor (int64 or object dtype for values beyond int64)."""
+
+    def __init__(self, values):
+        self.values = _as_values(values)
+
+    @property
+    def shape(self):
+        return self.values.shape
+
+    @property
+    def ndim(self):
+        return self.values.ndim
+
+    @property
+    def size(self):
+        return self.values.size
+
+    def __getitem__(self, item):
+        return PlaintextArray(self.values[item])
+
+    def to_numpy(self):
+        return self.values.copy()
+
+    def __str__(self):
+        return str(self.values)
+
+    __repr__ = __str__
+
+
+class CiphertextArray:
+    """Ciphertext tensor: limbs (size, S) in Montgomery form plus a shape."""
+
+    def __init__(self, kit, limbs, shape):
+        self.kit = kit
+        self.limbs = np.ascontiguousarray(limbs, dtype=np.uint32).reshape(-1, kit.key.ct_limbs)
+        self.shape = tuple(shape)
+        if int(np.prod(self.shape, dtype=np.int64)) != self.limbs.shape[0]:
+            raise ValueError("shape does not match the number of ciphertexts")
+
+    @property
+    def ndim(self):
+        return len(self.shape)
+
+    @property
+    def size(self):
+        return self.limbs.shape[0]
+
+    def __len__(self):
+        return self.shape[0]
+
+    def __getitem__(self, item):
+        idx = np.arange(self.size).reshape(self.shape)[item]
+        idx = np.asarray(idx)
+        return CiphertextArray(self.kit, self.limbs[idx.reshape(-1)], idx.shape)
+
+    def grid(self):
+        """limbs as (*shape, S)"""
+        return self.limbs.reshape(self.shape + (self.kit.key.ct_limbs,))
+
+    def __str__(self):
+        return f"CiphertextArray(shape={self.shape}, key_bits={self.kit.key.key_bits})"
+
+    __repr__ = __str__
+
+
+def setup(key_size=2048, seed=None, device=0, table_window=0, context=None):
+    """Key generation (key_generator.cc:26-60, seeded xoshiro256** stream; a
+    random seed when none is given) and engine key load -> HeKit."""
+    if seed is None:
+        seed = int.from_bytes(os.urandom(8), "little")
+    k = engine.keygen(key_size, seed)
+    ctx = context or engine.Context(device)
+    key = ctx.load_key(key_size, k["n"], k["h_s"], k["p"], k["q"], table_window=table_window)
+    return HeKit(ctx, key, k)
+
+
+class HeKit:
+    def __init__(self, ctx, key, key_ints):
+        self.context = ctx
+        self.key = key
+        self.public_key = {"n": key_ints["n"], "h_s": key_ints["h_s"]}
+        self.secret_key = {"p": key_ints["p"], "q": key_ints["q"]}
+        self.n = key_ints["n"]
+
+    def array(self, values):
+        return PlaintextArray(values)
+
+    def encryptor(self, r_source=None):
+        return Encryptor(self, r_source)
+
+    def decryptor(self):
+        return Decryptor(self)
+
+    def evaluator(self):
+        return Evaluator(self)
+
+
+class Encryptor:
+    """Encrypt(PMatrix) (numpy/encryptor.cc:19-66).  r (k/2 bits,
+    encryptor.cc:27) comes from os.urandom, or from ``r_source(count)``
+    returning a (count, r_limbs) uint32 array when one is given."""
+
+    def __init__(self, kit, r_source=None):
+        self.kit = kit
+        self.r_source = r_source
+
+    def _r(self, count):
+        key = self.kit.key
+        if self.r_source is not None:
+            return np.ascontiguousarray(self.r_source(count), dtype=np.uint32).reshape(count, key.r_limbs)
+        r = np.frombuffer(os.urandom(count * key.r_limbs * 4), dtype=np.uint32).reshape(count, key.r_limbs).copy()
+        return r
+
+    def encrypt(self, pt):
+        pt = pt if isinstance(pt, PlaintextArray) else PlaintextArray(pt)
+        key = self.kit.key
+        flat = pt.values.reshape(-1)
+        if flat.dtype == object:
+            half = self.kit.n // 2
+            if any(abs(int(v)) > half for v in flat):
+                raise ValueError("message number out of range")
+            limbs = key.encrypt_bn([int(v) for v in flat], self._r(flat.size))
+        else:
+            limbs = key.encrypt(flat, self._r(flat.size))
+        return CiphertextArray(self.kit, limbs, pt.shape)
+
+    def encrypt_zero(self, shape=()):
+        count = int(np.prod(shape, dtype=np.int64))
+        return CiphertextArray(self.kit, self.kit.key.encrypt_zero(self._r(count)), shape)
+
+
+class Decryptor:
+    """Decrypt / DecryptInRange (numpy/decryptor.cc:19-99)."""
+
+    def __init__(self, kit):
+        self.kit = kit
+
+    def decrypt(self, ct):
+        key = self.kit.key
+        m, ovf = key.decrypt(ct.limbs)
+        if ovf.any():
+            vals = np.empty(ct.size, dtype=object)
+            vals[:] = key.decrypt_bn(ct.limbs)
+            return PlaintextArray(vals.reshape(ct.shape))
+        return PlaintextArray(m.reshape(ct.shape))
+
+    def decrypt_in_range(self, ct, range_bits=128):
+        vals = self.kit.key.decrypt_in_range(ct.limbs, range_bits)
+        if isinstance(vals, list):
+            out = np.empty(len(vals), dtype=object)
+            out[:] = vals
+            return PlaintextArray(out.reshape(ct.shape))
+        return PlaintextArray(np.asarray(vals).reshape(ct.shape))
+
+
+def _broadcast_index(shape_x, shape_y):
+    try:
+        out = np.broadcast_shapes(shape_x, shape_y)
+    except ValueError:
+        raise ValueError(f"operands could not be broadcast together: dim(x)={shape_x}, dim(y)={shape_y}")
+    ix = np.broadcast_to(np.arange(int(np.prod(shape_x, dtype=np.int64))).reshape(shape_x), out).reshape(-1)
+    iy = np.broadcast_to(np.arange(int(np.prod(shape_y, dtype=np.int64))).reshape(shape_y), out).reshape(-1)
+    return out, ix, iy
+
+
+class Evaluator:
+    """heu.numpy Evaluator (numpy/evaluator.h:23-87) on the engine."""
+
+    def __init__(self, kit):
+        self.kit = kit
+        self.key = kit.key
+
+    # -- element-wise ------------------------------------------------------
+    def _plain_i64(self, p, idx):
+        v = p.values.reshape(-1)[idx]
+        if v.dtype == object:
+            return None, v
+        return np.ascontiguousarray(v, dtype=np.int64), None
+
+    def add(self, x, y):
+        if isinstance(x, PlaintextArray) and isinstance(y, PlaintextArray):
+            return PlaintextArray(_as_values(x.values.astype(object) + y.values.astype(object)))
+        if isinstance(x, PlaintextArray):
+            x, y = y, x
+        shape, ix, iy = _broadcast_index(x.shape, y.shape)
+        a = x.limbs[ix]
+        if isinstance(y, CiphertextArray):
+            return CiphertextArray(self.kit, self.key.add(a, y.limbs[iy]), shape)
+        p64, big = self._plain_i64(y, iy)
+        if p64 is not None:
+            return CiphertextArray(self.kit, self.key.add_plain(a, p64), shape)
+        # full-range addends: (1 + p*n) is the encryption of p with r = 0
+        g = self.key.encrypt_bn([int(v) for v in big], np.zeros((len(big), self.key.r_limbs), np.uint32))
+        return CiphertextArray(self.kit, self.key.add(a, g), shape)
+
+    def sub(self, x, y):
+        """Sub (numpy/evaluator.cc:160-185 over evaluator.cc:66-84)."""
+        if isinstance(x, PlaintextArray) and isinstance(y, PlaintextArray):
+            return PlaintextArray(_as_values(x.values.astype(object) - y.values.astype(object)))
+        if isinstance(y, PlaintextArray):
+            return self.add(x, PlaintextArray(_as_values(-y.values.astype(object))))
+        shape, ix, iy = _broadcast_index(x.shape, y.shape)
+        if isinstance(x, CiphertextArray):
+            return CiphertextArray(self.kit, self.key.sub(x.limbs[ix], y.limbs[iy]), shape)
+        neg = CiphertextArray(self.kit, self.key.negate(y.limbs[iy]), shape)
+        return self.add(neg, PlaintextArray(x.values.reshape(-1)[ix].reshape(shape)))
+
+    def mul(self, x, y):
+        if isinstance(x, PlaintextArray) and isinstance(y, PlaintextArray):
+            return PlaintextArray(_as_values(x.values.astype(object) * y.values.astype(object)))
+        if isinstance(x, PlaintextArray):
+            x, y = y, x
+        if not isinstance(y, PlaintextArray):
+            raise TypeError("ciphertext * ciphertext is not defined for Paillier")
+        shape, ix, iy = _broadcast_index(x.shape, y.shape)
+        p64, big = self._plain_i64(y, iy)
+        if p64 is None:
+            raise ValueError("scalars must fit int64 for ciphertext multiplication")
+        return CiphertextArray(self.kit, self.key.mul(x.limbs[ix], p64), shape)
+
+    def negate(self, x):
+        return CiphertextArray(self.kit, self.key.negate(x.limbs), x.shape)
+
+    def randomize(self, x, r=None):
+        r = r if r is not None else Encryptor(self.kit)._r(x.size)
+        return CiphertextArray(self.kit, self.key.randomize(x.limbs, r), x.shape)
+
+    # -- reductions --------------------------------------------------------
+    def sum(self, x):
+        """Sum of all elements (numpy/evaluator.cc:355-373)."""
+        if isinstance(x, PlaintextArray):
+            return int(np.sum(x.values.astype(object)))
+        if x.size == 0:
+            raise ValueError("you cannot sum an empty tensor")
+        return CiphertextArray(self.kit, self.key.sum(x.limbs), ())
+
+    def select_sum(self, x, item):
+        """Sum of x[item] (extension_functions.cc:28-58)."""
+        if isinstance(x, PlaintextArray):
+            return int(np.sum(np.asarray(x.values[item]).astype(object)))
+        if x.size == 0:
+            raise ValueError(f"you cannot select sum an empty tensor, shape={x.shape}")
+        sub = x[item]
+        if sub.size == 0:
+            return CiphertextArray(self.kit, self.key._identity(), ())
+        return CiphertextArray(self.kit, self.key.sum(sub.limbs), ())
+
+    def batch_select_sum(self, x, items):
+        """[select_sum(x, it) for it in items] (extension_functions.cc:60-78),
+        grouped into bucket-sum launches of up to 256 selections."""
+        if isinstance(x, PlaintextArray):
+            return PlaintextArray(_as_values([self.select_sum(x, it) for it in items]))
+        if x.size == 0:
+            raise ValueError(f"you cannot select sum an empty tensor, shape={x.shape}")
+        idx = np.arange(x.size).reshape(x.shape)
+        sels = [np.asarray(idx[it]).reshape(-1) for it in items]
+        out = self.key.batch_select_sum(x.limbs, sels)
+        return CiphertextArray(self.kit, out, (len(items),))
+
+    def feature_wise_bucket_sum(self, x, subgroup_map, order_map, bucket_num, cumsum=False):
+        """FeatureWiseBucketSum over the rows selected by subgroup_map
+        (extension_functions.cc:89-107; numpy/evaluator.cc:378-458).
+        Returns (bucket_num * features, cols)."""
+        rows = np.nonzero(np.asarray(subgroup_map).reshape(-1) > 0)[0]
+        om = np.asarray(order_map)
+        grid = x.grid() if x.ndim == 2 else x.grid().reshape(x.shape[0], 1, -1)
+        feats = om.shape[1]
+        cols = grid.shape[1]
+        if len(rows) == 0:
+            zero = self.key._identity()
+            return CiphertextArray(self.kit, np.repeat(zero, bucket_num * feats * cols, axis=0),
+                                   (bucket_num * feats, cols))
+        out = self.key.bucket_sum(grid[rows], om[rows].astype(np.uint8), bucket_num, cumsum=cumsum)
+        return CiphertextArray(self.kit, out.reshape(-1, self.key.ct_limbs), (bucket_num * feats, cols))
+
+    def batch_feature_wise_bucket_sum(self, x, subgroup_maps, order_map, bucket_num, cumsum=False):
+        """One feature_wise_bucket_sum per subgroup map (extension_functions.cc:109-138)."""
+        return [self.feature_wise_bucket_sum(x, sm, order_map, bucket_num, cumsum) for sm in subgroup_maps]
+
+    def matmul(self, x, y):
+        """MatMul (numpy/evaluator.cc:208-353): ciphertext @ plaintext or
+        plaintext @ ciphertext, with NumPy's 1-D rules ((K,) @ (K, N) -> (N,),
+        (M, K) @ (K,) -> (M,))."""
+        if isinstance(x, CiphertextArray) and isinstance(y, PlaintextArray):
+            xv = x.grid() if x.ndim == 2 else x.grid().reshape(1, x.shape[0], -1)
+            yv = np.asarray(y.values, dtype=np.int64)
+            yv = yv if yv.ndim == 2 else yv.reshape(-1, 1)
+            out = self.key.matmul(xv, yv)
+        elif isinstance(x, PlaintextArray) and isinstance(y, CiphertextArray):
+            # (P @ C)^T = C^T @ P^T
+            yv = y.grid() if y.ndim == 2 else y.grid().reshape(y.shape[0], 1, -1)
+            ct_t = np.ascontiguousarray(np.transpose(yv, (1, 0, 2)))
+            pv = np.asarray(x.values, dtype=np.int64)
+            pv = pv if pv.ndim == 2 else pv.reshape(1, -1)
+            out = np.ascontiguousarray(np.transpose(self.key.matmul(ct_t, np.ascontiguousarray(pv.T)), (1, 0, 2)))
+        else:
+            raise TypeError("matmul needs one ciphertext and one plaintext operand")
+        shape = out.shape[:2]
+        if x.ndim == 1:
+            shape = shape[1:]
+        if y.ndim == 1:
+            shape = shape[:-1]
+        return CiphertextArray(self.kit, out.reshape(-1, self.key.ct_limbs), shape)
