@@ -390,19 +390,51 @@ def ours_arm(args):
         d_h = torch.empty((n,), dtype=torch.int64, **pin)
         o_h = torch.empty((n,), dtype=torch.uint8, **pin)
 
+        e2e_op_s = {"encrypt": 0.0, "add": 0.0, "mul": 0.0, "decrypt": 0.0}
+        e2e_trace = []
+
         def e2e_step():
+            t = time.perf_counter()
             capi.check(lib.hg_encrypt(h, key.id, P(m_h), P(r_h), P(ct_h), n))
+            t1 = time.perf_counter()
             capi.check(lib.hg_add(h, key.id, P(ct_h), P(ct2_h), P(cs_h), n))
+            t2 = time.perf_counter()
             capi.check(lib.hg_mul(h, key.id, P(ct_h), P(k_h), P(cm_hh), n))
+            t3 = time.perf_counter()
             capi.check(lib.hg_decrypt(h, key.id, P(cs_h), P(d_h), P(o_h), n))
+            t4 = time.perf_counter()
+            for nm, dt in zip(("encrypt", "add", "mul", "decrypt"), (t1 - t, t2 - t1, t3 - t2, t4 - t3)):
+                e2e_op_s[nm] += dt
+            e2e_trace.append([round(t1 - t, 4), round(t2 - t1, 4), round(t3 - t2, 4), round(t4 - t3, 4)])
 
         e2e_step()
+        for nm in e2e_op_s:
+            e2e_op_s[nm] = 0.0
         if dist:
             dist.barrier()
         t = time.perf_counter()
         for _ in range(args.e2e_steps):
             e2e_step()
         e2e_dt = time.perf_counter() - t
+        # raw pinned copy bandwidth on this host, for reading the e2e overhead
+        big = torch.empty((n, S), dtype=torch.int32, pin_memory=True)
+        dbig = torch.empty((n, S), dtype=torch.int32, device=dev)
+        torch.cuda.synchronize()
+        tc = time.perf_counter()
+        dbig.copy_(big, non_blocking=True)
+        torch.cuda.synchronize()
+        h2d_gbs = big.numel() * 4 / (time.perf_counter() - tc) / 1e9
+        tc = time.perf_counter()
+        big.copy_(dbig, non_blocking=True)
+        torch.cuda.synchronize()
+        d2h_gbs = big.numel() * 4 / (time.perf_counter() - tc) / 1e9
+        del big, dbig
+        # the same copies as the engine's runtime sees them
+        seen = {}
+        for nm, buf, dr in (("ct_in_h2d", ct2_h, 0), ("ct_out_d2h", cs_h, 1)):
+            mt, g = ctypes.c_int(), ctypes.c_double()
+            rc = lib.hg_probe_host_copy(local, P(buf), buf.numel() * 4, dr, ctypes.byref(mt), ctypes.byref(g))
+            seen[nm] = {"rc": rc, "mem_type": mt.value, "gbs": g.value}
         if dist:
             tt = torch.tensor([e2e_dt], device=dev, dtype=torch.float64)
             dist.all_reduce(tt, op=dist.ReduceOp.MAX)
@@ -414,7 +446,10 @@ def ours_arm(args):
         d2h = n * cb * 3 + n * 9
         e2e = {"value": 4 * n * world * args.e2e_steps / e2e_dt, "unit": UNIT, "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h, "steps": args.e2e_steps,
-               "api": "hg_encrypt/hg_add/hg_mul/hg_decrypt (host pointers, pinned)"}
+               "api": "hg_encrypt/hg_add/hg_mul/hg_decrypt (host pointers, pinned)",
+               "per_op_s": {k: v / args.e2e_steps for k, v in e2e_op_s.items()},
+               "trace_s": e2e_trace,
+               "pinned_copy_gbs": {"h2d": h2d_gbs, "d2h": d2h_gbs, "engine_runtime": seen}}
 
     # per-call latency of small host-pointer calls (no per-call allocation:
     # staging buffers and streams belong to the context)

@@ -114,3 +114,37 @@ extern "C" int hg_probe_mac_peak(int device, int pattern, double* macs_per_secon
   if (seconds) *seconds = ms * 1e-3 / reps;
   return 0;
 }
+
+extern "C" int hg_probe_host_copy(int device, void* host, size_t bytes, int dir, int* mem_type, double* gbs) {
+  if (!host || !mem_type || !gbs || bytes == 0) return 1;
+  if (cudaSetDevice(device) != cudaSuccess) return 2;
+  cudaPointerAttributes pa{};
+  *mem_type = (cudaPointerGetAttributes(&pa, host) == cudaSuccess) ? (int)pa.type : -1;
+  cudaGetLastError();
+  void* d = nullptr;
+  if (cudaMalloc(&d, bytes) != cudaSuccess) return 3;
+  cudaStream_t st;
+  cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  // one untimed copy, then the timed one
+  for (int it = 0; it < 2; ++it) {
+    if (it) cudaEventRecord(a, st);
+    if (dir == 0)
+      cudaMemcpyAsync(d, host, bytes, cudaMemcpyHostToDevice, st);
+    else
+      cudaMemcpyAsync(host, d, bytes, cudaMemcpyDeviceToHost, st);
+    if (it) cudaEventRecord(b, st);
+  }
+  const cudaError_t e = cudaEventSynchronize(b);
+  float ms = 0.0f;
+  cudaEventElapsedTime(&ms, a, b);
+  *gbs = ms > 0.0f ? (double)bytes / (ms * 1e-3) / 1e9 : 0.0;
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaStreamDestroy(st);
+  cudaFree(d);
+  return e == cudaSuccess ? 0 : 4;
+}
+

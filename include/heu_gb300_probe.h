@@ -20,6 +20,12 @@ int hg_probe_mac_peak(int device, int pattern, double* macs_per_second, double* 
 /* Number of engine kernels this process has launched so far. */
 int hg_probe_launch_count(uint64_t* out);
 
+/* How the engine's CUDA runtime sees a host pointer (the
+ * cudaPointerAttributes type: 0 unregistered, 1 pinned host, 2 device,
+ * 3 managed) and the bandwidth of one `bytes` copy between it and a fresh
+ * device buffer on `device` (dir 0: host to device, 1: device to host). */
+int hg_probe_host_copy(int device, void* host, size_t bytes, int dir, int* mem_type, double* gbs);
+
 /* Open-loop load generator for the request server: Poisson arrivals at
  * `rate`/s, lengths log-uniform in [len_min, len_max], keys uniform over
  * key_ids, ops drawn with op_weights over (encrypt, add, mul, sum, decrypt);

@@ -302,3 +302,35 @@ def test_config1_workflow_bit_exact_against_c_restatement(gpu_key):
     assert np.array_equal(d, (m + m[nxt]) * k)
     d_c, _ = ck.decrypt(p_c[:256], threads=th)
     assert np.array_equal(d[:256], d_c)
+
+
+def test_empty_batches_and_ragged_tails(kk):
+    """count = 0 is a no-op for every element-wise call; Sum of nothing is an
+    error as in numpy/evaluator.cc (you cannot sum an empty tensor); batch
+    sizes that leave partial warps and partial groups match the oracle."""
+    key, pk, sk = kk
+    S, RL = key.ct_limbs, key.r_limbs
+    e_ct = np.zeros((0, S), np.uint32)
+    assert key.encrypt(np.zeros(0, np.int64), np.zeros((0, RL), np.uint32)).shape == (0, S)
+    m, ovf = key.decrypt(e_ct)
+    assert m.shape == (0,) and ovf.shape == (0,)
+    assert key.add(e_ct, e_ct).shape == (0, S)
+    assert key.sub(e_ct, e_ct).shape == (0, S)
+    assert key.mul(e_ct, np.zeros(0, np.int64)).shape == (0, S)
+    assert key.negate(e_ct).shape == (0, S)
+    assert key.add_plain(e_ct, np.zeros(0, np.int64)).shape == (0, S)
+    with pytest.raises(hg.HgError):
+        key.sum(e_ct)
+    prg = Prg(77)
+    for count in (1, 3, 5, 33, 65):
+        ms = rand_i64(prg, count, -(2 ** 50), 2 ** 50)
+        ks = rand_i64(prg, count)
+        rs = pz.r_stream(700 + count, count, pk.key_size // 2)
+        zs = [pz.encrypt(pk, m, r) for m, r in zip(ms, rs)]
+        ct = key.encrypt(np.array(ms, dtype=np.int64), r_limbs(pk, rs, key))
+        assert_ct_equal(pk, key, ct, zs, f"encrypt[{count}]")
+        d, ovf = key.decrypt(ct)
+        assert d.tolist() == ms and ovf.sum() == 0
+        assert_ct_equal(pk, key, key.mul(ct, np.array(ks, dtype=np.int64)),
+                        [pz.mul(pk, z, k) for z, k in zip(zs, ks)], f"mul[{count}]")
+        assert_ct_equal(pk, key, key.negate(ct), [pz.negate(pk, z) for z in zs], f"negate[{count}]")
