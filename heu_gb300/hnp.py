@@ -100,6 +100,56 @@ class CiphertextArray:
     __repr__ = __str__
 
 
+class BatchEncoder:
+    """Two integers per plaintext (phe/encoding/batch_encoder.h:27-140):
+    plaintext = (second << (64 + padding_bits)) | first, each value scaled and
+    taken as its 64-bit two's-complement bit pattern; padding bits absorb the
+    carries of additions.  Packing and unpacking work on limb arrays (NumPy,
+    no per-element Python integers), so a packed vector costs one ciphertext
+    per pair of values."""
+
+    def __init__(self, scale=1, padding_bits=32):
+        if padding_bits % 32:
+            raise ValueError("padding_bits must be a multiple of 32 here (limb-aligned packing)")
+        self.scale = int(scale)
+        self.padding_bits = int(padding_bits)
+
+    def _limbs_needed(self):
+        return (128 + self.padding_bits) // 32
+
+    def pack(self, first, second, pt_limbs):
+        """int64 arrays -> (count, pt_limbs) uint32 magnitudes."""
+        a = (np.asarray(first, dtype=np.int64) * self.scale).astype(np.int64).view(np.uint64)
+        b = (np.asarray(second, dtype=np.int64) * self.scale).astype(np.int64).view(np.uint64)
+        if a.shape != b.shape:
+            raise ValueError("first and second must have the same shape")
+        need = self._limbs_needed()
+        if need > pt_limbs:
+            raise ValueError("key too small for this padding")
+        out = np.zeros((a.size, pt_limbs), dtype=np.uint32)
+        out[:, 0] = (a.reshape(-1) & 0xFFFFFFFF).astype(np.uint32)
+        out[:, 1] = (a.reshape(-1) >> np.uint64(32)).astype(np.uint32)
+        off = (64 + self.padding_bits) // 32
+        out[:, off] = (b.reshape(-1) & 0xFFFFFFFF).astype(np.uint32)
+        out[:, off + 1] = (b.reshape(-1) >> np.uint64(32)).astype(np.uint32)
+        return out
+
+    def unpack(self, mags, index):
+        """(count, pt_limbs) magnitudes -> int64 values of slot `index` (0 or 1)
+        divided by the scale (Decode, batch_encoder.h:85-103)."""
+        if index not in (0, 1):
+            raise ValueError("You cannot get more than two elements from one plaintext")
+        off = index * ((64 + self.padding_bits) // 32)
+        lo = mags[:, off].astype(np.uint64)
+        hi = mags[:, off + 1].astype(np.uint64)
+        v = (lo | (hi << np.uint64(32))).view(np.int64)
+        if self.scale == 1:
+            return v
+        q = np.abs(v) // self.scale  # C++ division truncates toward zero
+        return np.where(v < 0, -q, q)
+
+
+
 def setup(key_size=2048, seed=None, device=0, table_window=0, context=None):
     """Key generation (key_generator.cc:26-60, seeded xoshiro256** stream; a
     random seed when none is given) and engine key load -> HeKit."""
@@ -130,6 +180,9 @@ class HeKit:
 
     def evaluator(self):
         return Evaluator(self)
+
+    def batch_encoder(self, scale=1, padding_bits=32):
+        return BatchEncoder(scale, padding_bits)
 
 
 class Encryptor:
@@ -165,6 +218,17 @@ class Encryptor:
         count = int(np.prod(shape, dtype=np.int64))
         return CiphertextArray(self.kit, self.kit.key.encrypt_zero(self._r(count)), shape)
 
+    def encrypt_batch(self, first, second, encoder):
+        """Encrypt pairs packed by a BatchEncoder -> CiphertextArray of first's shape."""
+        key = self.kit.key
+        mags = encoder.pack(first, second, key.pt_limbs)
+        neg = np.zeros(mags.shape[0], dtype=np.uint8)
+        r = self._r(mags.shape[0])
+        out = np.empty((mags.shape[0], key.ct_limbs), dtype=np.uint32)
+        engine.capi.check(key.lib.hg_encrypt_bn(key.ctx.handle, key.id, engine._ptr(mags), engine._ptr(neg),
+                                                engine._ptr(r), engine._ptr(out), mags.shape[0]))
+        return CiphertextArray(self.kit, out, np.asarray(first).shape)
+
 
 class Decryptor:
     """Decrypt / DecryptInRange (numpy/decryptor.cc:19-99)."""
@@ -180,6 +244,17 @@ class Decryptor:
             vals[:] = key.decrypt_bn(ct.limbs)
             return PlaintextArray(vals.reshape(ct.shape))
         return PlaintextArray(m.reshape(ct.shape))
+
+    def decrypt_batch(self, ct, encoder):
+        """Decrypt packed ciphertexts -> (first, second) int64 arrays."""
+        key = self.kit.key
+        mag = np.empty((ct.size, key.pt_limbs), dtype=np.uint32)
+        neg = np.empty(ct.size, dtype=np.uint8)
+        engine.capi.check(key.lib.hg_decrypt_bn(key.ctx.handle, key.id, engine._ptr(ct.limbs), engine._ptr(mag),
+                                                engine._ptr(neg), ct.size))
+        if neg.any():
+            raise ValueError("packed plaintext is negative: a slot underflowed its padding")
+        return encoder.unpack(mag, 0).reshape(ct.shape), encoder.unpack(mag, 1).reshape(ct.shape)
 
     def decrypt_in_range(self, ct, range_bits=128):
         vals = self.kit.key.decrypt_in_range(ct.limbs, range_bits)

@@ -130,3 +130,23 @@ def test_matmul_both_ways(kit):
     v = rng.integers(-9, 9, size=4)
     cm = enc.encrypt(kit.array(rng.integers(-9, 9, size=(3, 4))))
     assert ev.matmul(cm, kit.array(v)).shape == (3,)
+
+
+def test_batch_encoder_packed_ciphertexts(kit):
+    """Two int64 per ciphertext (phe/encoding/batch_encoder.h): encrypt packed,
+    add and sum slot-wise, scale by a small positive scalar."""
+    enc, dec, ev = kit.encryptor(), kit.decryptor(), kit.evaluator()
+    be = kit.batch_encoder()
+    rng = np.random.default_rng(12)
+    a1, b1 = rng.integers(-(2 ** 40), 2 ** 40, size=(2, 300))
+    a2, b2 = rng.integers(-(2 ** 40), 2 ** 40, size=(2, 300))
+    c1 = enc.encrypt_batch(a1, b1, be)
+    c2 = enc.encrypt_batch(a2, b2, be)
+    f, s = dec.decrypt_batch(c1, be)
+    assert np.array_equal(f, a1) and np.array_equal(s, b1)
+    f, s = dec.decrypt_batch(ev.add(c1, c2), be)
+    assert np.array_equal(f, a1 + a2) and np.array_equal(s, b1 + b2)
+    f, s = dec.decrypt_batch(ev.sum(c1), be)
+    assert int(f) == int(a1.sum()) and int(s) == int(b1.sum())
+    f, s = dec.decrypt_batch(ev.mul(c1, kit.array(np.full(300, 3))), be)
+    assert np.array_equal(f, a1 * 3) and np.array_equal(s, b1 * 3)

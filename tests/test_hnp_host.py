@@ -29,3 +29,24 @@ def test_broadcast_index_maps():
     assert shape == (4,) and ix.tolist() == [0, 0, 0, 0]
     with pytest.raises(ValueError, match="broadcast"):
         hnp._broadcast_index((2, 3), (2,))
+
+
+def test_batch_encoder_packs_like_the_reference():
+    """DoEncode (batch_encoder.h:128-135): (second << (64 + pad)) | first on the
+    64-bit two's-complement patterns; Decode takes slot i's low 64 bits."""
+    e = hnp.BatchEncoder(scale=1, padding_bits=32)
+    a = np.array([1, -1, 2 ** 62, -(2 ** 63)], dtype=np.int64)
+    b = np.array([-5, 7, -(2 ** 40), 2 ** 63 - 1], dtype=np.int64)
+    m = e.pack(a, b, 32)
+    vals = [int.from_bytes(row.tobytes(), "little") for row in m]
+    assert vals == [((int(y) & (2 ** 64 - 1)) << 96) | (int(x) & (2 ** 64 - 1)) for x, y in zip(a, b)]
+    assert np.array_equal(e.unpack(m, 0), a) and np.array_equal(e.unpack(m, 1), b)
+    # slot-wise sums survive carries into the padding
+    s = vals[0] + vals[1]
+    mm = np.frombuffer(s.to_bytes(128, "little"), np.uint32).reshape(1, 32)
+    assert e.unpack(mm, 0).tolist() == [0] and e.unpack(mm, 1).tolist() == [2]
+    e10 = hnp.BatchEncoder(scale=10)
+    m10 = e10.pack([3, -4], [-7, 8], 32)
+    assert e10.unpack(m10, 0).tolist() == [3, -4] and e10.unpack(m10, 1).tolist() == [-7, 8]
+    with pytest.raises(ValueError):
+        e.unpack(m, 2)
