@@ -67,6 +67,13 @@ SIGNATURES = {
     "hg_dev_add": [_P, _I, _P, _P, _P, _SZ, _P],
     "hg_dev_mul": [_P, _I, _P, _P, _P, _SZ, _P],
     "hg_dev_sum": [_P, _I, _P, _SZ, _P, _P],
+    "hg_dev_encrypt_zero": [_P, _I, _P, _P, _SZ, _P],
+    "hg_dev_randomize": [_P, _I, _P, _P, _SZ, _P],
+    "hg_dev_add_plain": [_P, _I, _P, _P, _P, _SZ, _P],
+    "hg_dev_sub_plain": [_P, _I, _P, _P, _P, _SZ, _P],
+    "hg_dev_plain_sub": [_P, _I, _P, _P, _P, _SZ, _P],
+    "hg_dev_sub": [_P, _I, _P, _P, _P, _SZ, _P],
+    "hg_dev_negate": [_P, _I, _P, _P, _SZ, _P],
     "hg_dev_sum_noalloc": [_P, _I, _P, _SZ, _P, _P],
     "hg_dev_check": [_P],
     "hg_bucket_sum": [_P, _I, _P, _SZ, _SZ, _P, _SZ, _I, _I, _P],

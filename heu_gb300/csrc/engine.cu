@@ -1107,6 +1107,80 @@ int hg_dev_mul(hg_ctx* ctx, int key_id, const uint32_t* a, const int64_t* kk, ui
   });
 }
 
+int hg_dev_encrypt_zero(hg_ctx* ctx, int key_id, const uint32_t* r, uint32_t* ct_out, size_t count, void* stream) {
+  return guarded([&] {
+    HG_DEV_PROLOGUE
+    core_encrypt(*k, w, hg::EncMode::kZero, nullptr, nullptr, nullptr, r, nullptr, ct_out, count);
+    return HG_OK;
+  });
+}
+
+int hg_dev_randomize(hg_ctx* ctx, int key_id, uint32_t* ct, const uint32_t* r, size_t count, void* stream) {
+  return guarded([&] {
+    HG_DEV_PROLOGUE
+    core_encrypt(*k, w, hg::EncMode::kRandomize, nullptr, nullptr, nullptr, r, ct, ct, count);
+    return HG_OK;
+  });
+}
+
+int hg_dev_add_plain(hg_ctx* ctx, int key_id, const uint32_t* a, const int64_t* p, uint32_t* out, size_t count,
+                     void* stream) {
+  return guarded([&] {
+    HG_DEV_PROLOGUE
+    cuda_check(hg::launch_add_plain(k->S, k->kc, a, p, 0, out, count, w.errp(), w.stream), "add_plain launch");
+    return HG_OK;
+  });
+}
+
+int hg_dev_sub_plain(hg_ctx* ctx, int key_id, const uint32_t* a, const int64_t* p, uint32_t* out, size_t count,
+                     void* stream) {
+  return guarded([&] {
+    HG_DEV_PROLOGUE
+    cuda_check(hg::launch_add_plain(k->S, k->kc, a, p, 1, out, count, w.errp(), w.stream), "add_plain launch");
+    return HG_OK;
+  });
+}
+
+// out = a^-1: copy a into out (unless aliased), then invert in place
+static void dev_negate_into(KeyRec& k, Work& w, const uint32_t* a, uint32_t* out, size_t count) {
+  if (a != out)
+    cuda_check(cudaMemcpyAsync(out, a, count * ct_bytes(k), cudaMemcpyDeviceToDevice, w.stream), "copy");
+  core_inverse(k, w, out, nullptr, out, count);
+}
+
+int hg_dev_negate(hg_ctx* ctx, int key_id, const uint32_t* a, uint32_t* out, size_t count, void* stream) {
+  return guarded([&] {
+    HG_DEV_PROLOGUE
+    dev_negate_into(*k, w, a, out, count);
+    return HG_OK;
+  });
+}
+
+int hg_dev_plain_sub(hg_ctx* ctx, int key_id, const int64_t* p, const uint32_t* a, uint32_t* out, size_t count,
+                     void* stream) {
+  return guarded([&] {
+    HG_DEV_PROLOGUE
+    // evaluator.cc:82-84: Add(Negate(a), p)
+    dev_negate_into(*k, w, a, out, count);
+    cuda_check(hg::launch_add_plain(k->S, k->kc, out, p, 0, out, count, w.errp(), w.stream), "add_plain launch");
+    return HG_OK;
+  });
+}
+
+int hg_dev_sub(hg_ctx* ctx, int key_id, const uint32_t* a, const uint32_t* b, uint32_t* out, size_t count,
+               void* stream) {
+  return guarded([&] {
+    HG_DEV_PROLOGUE
+    // evaluator.cc:66-68: Add(a, Negate(b)); with out == a the inverse goes
+    // through the context's staging buffer so a is not overwritten first
+    uint32_t* nb = out;
+    if (out == a) nb = w.io[5].ensure<uint32_t>(count * ct_bytes(*k));
+    dev_negate_into(*k, w, b, nb, count);
+    cuda_check(hg::launch_add(k->S, k->kc, a, nb, out, count, w.errp(), w.stream), "add launch");
+    return HG_OK;
+  });
+}
+
 int hg_dev_sum(hg_ctx* ctx, int key_id, const uint32_t* a, size_t count, uint32_t* out, void* stream) {
   return guarded([&] {
     if (count == 0) fail(HG_ERR_INVALID, "you cannot sum an empty tensor");

@@ -250,6 +250,20 @@ int hg_dev_add(hg_ctx* ctx, int key_id, const uint32_t* a, const uint32_t* b, ui
 int hg_dev_mul(hg_ctx* ctx, int key_id, const uint32_t* a, const int64_t* k, uint32_t* out, size_t count,
                void* stream);
 int hg_dev_sum(hg_ctx* ctx, int key_id, const uint32_t* a, size_t count, uint32_t* out, void* stream);
+/* EncryptZero / Randomize (encryptor.cc:26-33, evaluator.cc:25-28); ct is updated in place */
+int hg_dev_encrypt_zero(hg_ctx* ctx, int key_id, const uint32_t* r, uint32_t* ct_out, size_t count, void* stream);
+int hg_dev_randomize(hg_ctx* ctx, int key_id, uint32_t* ct, const uint32_t* r, size_t count, void* stream);
+/* Add(ct, pt), Sub(ct, pt), Sub(pt, ct), Sub(ct, ct), Negate (evaluator.cc:46-97);
+ * out may alias a */
+int hg_dev_add_plain(hg_ctx* ctx, int key_id, const uint32_t* a, const int64_t* p, uint32_t* out, size_t count,
+                     void* stream);
+int hg_dev_sub_plain(hg_ctx* ctx, int key_id, const uint32_t* a, const int64_t* p, uint32_t* out, size_t count,
+                     void* stream);
+int hg_dev_plain_sub(hg_ctx* ctx, int key_id, const int64_t* p, const uint32_t* a, uint32_t* out, size_t count,
+                     void* stream);
+int hg_dev_sub(hg_ctx* ctx, int key_id, const uint32_t* a, const uint32_t* b, uint32_t* out, size_t count,
+               void* stream);
+int hg_dev_negate(hg_ctx* ctx, int key_id, const uint32_t* a, uint32_t* out, size_t count, void* stream);
 /* Allocation-free Sum.  No counterpart in the reference.  For callers that
  * cannot call cudaMalloc (device memory owned by another allocator or
  * reserved up front): same result as hg_dev_sum, but the partial products

@@ -334,3 +334,58 @@ def test_empty_batches_and_ragged_tails(kk):
         assert_ct_equal(pk, key, key.mul(ct, np.array(ks, dtype=np.int64)),
                         [pz.mul(pk, z, k) for z, k in zip(zs, ks)], f"mul[{count}]")
         assert_ct_equal(pk, key, key.negate(ct), [pz.negate(pk, z) for z in zs], f"negate[{count}]")
+
+
+def test_device_pointer_forms_match_host_forms(gpu_key):
+    """hg_dev_* on device buffers (one caller stream) give the host forms'
+    bytes: encrypt_zero, randomize, add_plain, sub_plain, plain_sub, sub
+    (including out aliasing a), negate."""
+    import ctypes
+
+    torch = pytest.importorskip("torch")
+    key, pk, sk = gpu_key(2048, 0)
+    lib, h = key.lib, key.ctx.handle
+    n = 37
+    prg = Prg(91)
+    ms = rand_i64(prg, n, -(2 ** 40), 2 ** 40)
+    ps = rand_i64(prg, n, -(2 ** 40), 2 ** 40)
+    rs = pz.r_stream(92, n, pk.key_size // 2)
+    r = r_limbs(pk, rs, key)
+    a = key.encrypt(np.array(ms, dtype=np.int64), r)
+    b = key.encrypt(np.array(ps, dtype=np.int64), r[::-1].copy())
+    dev = torch.device("cuda", 0)
+    st = torch.cuda.Stream(device=dev)
+    sp = ctypes.c_void_p(st.cuda_stream)
+    T = lambda x: torch.from_numpy(np.ascontiguousarray(x).view(np.int32)).to(dev)  # noqa: E731
+    P = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+    H = lambda t: t.cpu().numpy().view(np.uint32)  # noqa: E731
+    da, db, dr, dp = T(a), T(b), T(r), torch.from_numpy(np.array(ps, dtype=np.int64)).to(dev)
+    out = torch.empty_like(da)
+    with torch.cuda.stream(st):
+        capi.check(lib.hg_dev_encrypt_zero(h, key.id, P(dr), P(out), n, sp))
+        torch.cuda.synchronize()
+        assert np.array_equal(H(out), key.encrypt_zero(r))
+        rr = da.clone()
+        capi.check(lib.hg_dev_randomize(h, key.id, P(rr), P(dr), n, sp))
+        torch.cuda.synchronize()
+        assert np.array_equal(H(rr), key.randomize(a, r))
+        for fn, want in ((lib.hg_dev_add_plain, key.add_plain(a, ps)), (lib.hg_dev_sub_plain, key.sub_plain(a, ps))):
+            capi.check(fn(h, key.id, P(da), P(dp), P(out), n, sp))
+            torch.cuda.synchronize()
+            assert np.array_equal(H(out), want)
+        capi.check(lib.hg_dev_plain_sub(h, key.id, P(dp), P(da), P(out), n, sp))
+        torch.cuda.synchronize()
+        assert np.array_equal(H(out), key.plain_sub(ps, a))
+        capi.check(lib.hg_dev_sub(h, key.id, P(da), P(db), P(out), n, sp))
+        torch.cuda.synchronize()
+        assert np.array_equal(H(out), key.sub(a, b))
+        ac = da.clone()
+        capi.check(lib.hg_dev_sub(h, key.id, P(ac), P(db), P(ac), n, sp))
+        torch.cuda.synchronize()
+        assert np.array_equal(H(ac), key.sub(a, b))
+        capi.check(lib.hg_dev_negate(h, key.id, P(da), P(out), n, sp))
+        torch.cuda.synchronize()
+        assert np.array_equal(H(out), key.negate(a))
+    capi.check(lib.hg_dev_check(h))
+    d, _ = key.decrypt(H(ac))
+    assert d.tolist() == [x - y for x, y in zip(ms, ps)]
