@@ -100,6 +100,7 @@ SIGNATURES = {
     "hg_probe_serve_load": [_P, _P, _P, _P, _P, ctypes.POINTER(ctypes.c_double)],
     "hg_probe_mac_peak": [_I, _I, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)],
     "hg_probe_launch_count": [ctypes.POINTER(_U64)],
+    "hg_probe_set_alloc_limit": [_SZ, ctypes.POINTER(_SZ)],
     "hg_probe_host_copy": [_I, _P, ctypes.c_size_t, _I, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)],
 }
 

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <random>
 #include <condition_variable>
@@ -62,6 +63,12 @@ int guarded(F&& f) {
 }
 
 // grow-only device buffer
+// Device bytes held by engine buffers, and an optional cap on them (set by
+// hg_probe_set_alloc_limit to make allocation failures happen on purpose,
+// on the host, before cudaMalloc is called).
+std::atomic<size_t> g_dev_bytes{0};
+std::atomic<size_t> g_dev_limit{0};
+
 struct DevBuf {
   void* p = nullptr;
   size_t n = 0;
@@ -69,16 +76,26 @@ struct DevBuf {
   DevBuf(const DevBuf&) = delete;
   DevBuf& operator=(const DevBuf&) = delete;
   ~DevBuf() {
-    if (p) cudaFree(p);
+    if (p) {
+      cudaFree(p);
+      g_dev_bytes -= n;
+    }
   }
   template <typename T = void>
   T* ensure(size_t bytes) {
     if (bytes > n) {
-      if (p) cudaFree(p);
+      const size_t limit = g_dev_limit.load();
+      if (limit && g_dev_bytes.load() - n + bytes > limit)
+        fail(HG_ERR_NOMEM, "device allocation of " + std::to_string(bytes) + " bytes exceeds the set limit");
+      if (p) {
+        cudaFree(p);
+        g_dev_bytes -= n;
+      }
       p = nullptr;
       n = 0;
       cuda_check(cudaMalloc(&p, bytes), "cudaMalloc");
       n = bytes;
+      g_dev_bytes += n;
     }
     return reinterpret_cast<T*>(p);
   }
@@ -1965,6 +1982,12 @@ int hg_probe_serve_load(hg_server* s, const hg_load_spec* spec, double* latencie
     if (wall_s) *wall_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     return HG_OK;
   });
+}
+
+int hg_probe_set_alloc_limit(size_t bytes, size_t* held_bytes) {
+  g_dev_limit = bytes;
+  if (held_bytes) *held_bytes = g_dev_bytes.load();
+  return HG_OK;
 }
 
 int hg_probe_launch_count(uint64_t* out) {

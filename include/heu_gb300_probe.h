@@ -20,6 +20,12 @@ int hg_probe_mac_peak(int device, int pattern, double* macs_per_second, double* 
 /* Number of engine kernels this process has launched so far. */
 int hg_probe_launch_count(uint64_t* out);
 
+/* Failure injection on the host: caps the device bytes the engine's buffers
+ * may hold (0 = no cap).  A call whose buffers would pass the cap fails with
+ * HG_ERR_NOMEM before any cudaMalloc; the context stays usable.  Reports
+ * the bytes held now. */
+int hg_probe_set_alloc_limit(size_t bytes, size_t* held_bytes);
+
 /* How the engine's CUDA runtime sees a host pointer (the
  * cudaPointerAttributes type: 0 unregistered, 1 pinned host, 2 device,
  * 3 managed) and the bandwidth of one `bytes` copy between it and a fresh

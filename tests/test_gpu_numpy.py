@@ -189,3 +189,22 @@ def test_select_sum_and_batch_select_sum(gpu_key):
         assert zform(key, outs[i:i + 1]) == [want], i
     dec, _ = key.decrypt(outs)
     assert dec.tolist() == [int(sum(vals[r, 1] for r in s)) for s in sels]
+
+
+def test_bucket_sum_equals_select_sum_per_bucket(gpu_key):
+    """pylib numpy_test.py:469-560: every bucket of FeatureWiseBucketSum is the
+    select_sum of its rows — byte for byte here, since both are the same
+    product mod n^2."""
+    key, pk, sk = gpu_key(1024, 1)
+    rng = np.random.default_rng(21)
+    rows, feats, buckets = 120, 3, 6
+    vals = rng.integers(-10 ** 6, 10 ** 6, size=rows)
+    ct, _ = enc_matrix(key, pk, vals, 71)
+    om = rng.integers(0, buckets, size=(rows, feats)).astype(np.uint8)
+    out = key.bucket_sum(ct, om, buckets).reshape(feats * buckets, -1)
+    for f in range(feats):
+        for b in range(buckets):
+            sel = np.nonzero(om[:, f] == b)[0]
+            assert np.array_equal(out[f * buckets + b], key.select_sum(ct, sel).reshape(-1)), (f, b)
+    sels = [np.nonzero(om[:, f] == b)[0] for f in range(feats) for b in range(buckets)]
+    assert np.array_equal(key.batch_select_sum(ct, sels), out)

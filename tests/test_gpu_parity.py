@@ -389,3 +389,73 @@ def test_device_pointer_forms_match_host_forms(gpu_key):
     capi.check(lib.hg_dev_check(h))
     d, _ = key.decrypt(H(ac))
     assert d.tolist() == [x - y for x, y in zip(ms, ps)]
+
+
+def test_injected_allocation_failure_keeps_the_context_usable():
+    """Failure injection on the host: with a device-bytes cap set, a call whose
+    staging buffers would pass it fails with HG_ERR_NOMEM before any
+    cudaMalloc; after the cap is lifted the same call succeeds on the same
+    (fresh) context and key."""
+    import ctypes
+
+    pk, sk = oracle_key_small()
+    ctx = hg.Context(0)
+    try:
+        key = ctx.load_key(1024, pk.n, pk.h_s, sk.p, sk.q, table_window=6)
+        lib = key.lib
+        held = ctypes.c_size_t()
+        capi.check(lib.hg_probe_set_alloc_limit(0, ctypes.byref(held)))
+        n = 4096
+        m = np.arange(n, dtype=np.int64) - n // 2
+        r = np.ones((n, key.r_limbs), np.uint32)
+        try:
+            capi.check(lib.hg_probe_set_alloc_limit(held.value + 4096, None))
+            with pytest.raises(hg.HgError) as ei:
+                key.encrypt(m, r)
+            assert ei.value.code == capi.HG_ERR_NOMEM
+            assert "limit" in str(ei.value)
+        finally:
+            capi.check(lib.hg_probe_set_alloc_limit(0, None))
+        ct = key.encrypt(m, r)
+        d, ovf = key.decrypt(ct)
+        assert ovf.sum() == 0 and np.array_equal(d, m)
+        assert hg.limbs_to_ints(key.from_mont(ct[:2])) == [pz.encrypt(pk, int(v), 1) for v in m[:2]]
+    finally:
+        ctx.close()
+
+
+def oracle_key_small():
+    from tests.conftest import oracle_key
+
+    return oracle_key(1024, 1)
+
+
+def test_host_api_is_thread_safe(gpu_key):
+    """Vectorized calls arrive from many threads at once (numpy/encryptor.cc
+    parallel_for chunks); each host call takes one of the context's lanes."""
+    import threading
+
+    key, pk, sk = gpu_key(1024, 1)
+    errors = []
+
+    def worker(t):
+        try:
+            rng = np.random.default_rng(100 + t)
+            for it in range(6):
+                n = int(rng.integers(1, 3000))
+                m = rng.integers(-(2 ** 50), 2 ** 50, size=n)
+                r = rng.integers(0, 2 ** 32, size=(n, key.r_limbs), dtype=np.uint64).astype(np.uint32)
+                ct = key.encrypt(m, r)
+                k = rng.integers(-1000, 1000, size=n)
+                d, ovf = key.decrypt(key.mul(key.add(ct, ct), k))
+                if not (ovf.sum() == 0 and np.array_equal(d, 2 * m * k)):
+                    errors.append((t, it))
+        except Exception as e:  # collected for the main thread
+            errors.append(repr(e))
+
+    ths = [threading.Thread(target=worker, args=(t,)) for t in range(8)]
+    for t in ths:
+        t.start()
+    for t in ths:
+        t.join()
+    assert not errors, errors
