@@ -2,6 +2,7 @@
 // precompute and residency, device staging, and the multi-kernel sequences
 // (product-tree inverse, reduction levels, fixed-base table build).
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <atomic>
@@ -46,8 +47,16 @@ void cuda_check(cudaError_t e, const char* what) {
   }
 }
 
+// One NVTX range per C-ABI call (named after the entry point), so profilers
+// show the engine's calls on the timeline; free when no tool is attached.
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+};
+
 template <typename F>
-int guarded(F&& f) {
+int guarded(const char* name, F&& f) {
+  NvtxRange range(name);
   try {
     return f();
   } catch (const HgError& e) {
@@ -718,7 +727,7 @@ extern "C" {
 const char* hg_last_error(void) { return g_last_error.c_str(); }
 
 int hg_ctx_create(int device, hg_ctx** out) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     if (!out) fail(HG_ERR_INVALID, "null out pointer");
     auto ctx = std::make_unique<hg_ctx>();
     ctx->device = device;
@@ -737,7 +746,7 @@ int hg_ctx_create(int device, hg_ctx** out) {
 }
 
 int hg_ctx_destroy(hg_ctx* ctx) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     if (!ctx) return HG_OK;
     cudaSetDevice(ctx->device);
     cudaDeviceSynchronize();
@@ -750,7 +759,7 @@ int hg_device_sm_count(hg_ctx* ctx) { return ctx ? ctx->sm_count : 0; }
 
 int hg_keygen(uint32_t key_bits, uint64_t seed, uint32_t* n_out, uint32_t* p_out, uint32_t* q_out,
               uint32_t* hs_out) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     if (key_bits % 64 != 0 || key_bits < 128) fail(HG_ERR_INVALID, "Key size must be a multiple of 64");
     hg::Xoshiro prg(seed);
     const auto sp = small_primes();
@@ -788,7 +797,7 @@ int hg_keygen(uint32_t key_bits, uint64_t seed, uint32_t* n_out, uint32_t* p_out
 
 int hg_key_load(hg_ctx* ctx, uint32_t key_bits, const uint32_t* n, const uint32_t* h_s, const uint32_t* p,
                 const uint32_t* q, int table_window, int* key_id) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     if (!ctx || !n || !h_s || !key_id) fail(HG_ERR_INVALID, "null argument");
     if ((p == nullptr) != (q == nullptr)) fail(HG_ERR_INVALID, "give both p and q or neither");
     set_device(ctx);
@@ -798,7 +807,7 @@ int hg_key_load(hg_ctx* ctx, uint32_t key_bits, const uint32_t* n, const uint32_
 }
 
 int hg_key_free(hg_ctx* ctx, int key_id) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     if (!ctx) fail(HG_ERR_INVALID, "null context");
     set_device(ctx);
     cuda_check(cudaDeviceSynchronize(), "sync");
@@ -809,7 +818,7 @@ int hg_key_free(hg_ctx* ctx, int key_id) {
 }
 
 int hg_key_shape(hg_ctx* ctx, int key_id, int* ct_limbs, int* r_limbs, int* pt_limbs) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     KeyRec* k = get_key(ctx, key_id);
     if (ct_limbs) *ct_limbs = k->S;
     if (r_limbs) *r_limbs = k->kc.rlimbs;
@@ -830,7 +839,7 @@ int hg_key_shape(hg_ctx* ctx, int key_id, int* ct_limbs, int* r_limbs, int* pt_l
   (void)cb;
 
 int hg_encrypt(hg_ctx* ctx, int key_id, const int64_t* m, const uint32_t* r, uint32_t* ct_out, size_t count) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     if (!m || !r || !ct_out) fail(HG_ERR_INVALID, "null argument");
     HG_HOST_PROLOGUE
     const size_t rb = (size_t)k->kc.rlimbs * 4;
@@ -848,7 +857,7 @@ int hg_encrypt(hg_ctx* ctx, int key_id, const int64_t* m, const uint32_t* r, uin
 
 int hg_encrypt_bn(hg_ctx* ctx, int key_id, const uint32_t* m_mag, const uint8_t* m_neg, const uint32_t* r,
                   uint32_t* ct_out, size_t count) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     if (!m_mag || !m_neg || !r || !ct_out) fail(HG_ERR_INVALID, "null argument");
     HG_HOST_PROLOGUE
     const size_t rb = (size_t)k->kc.rlimbs * 4, pb = (size_t)k->S / 2 * 4;
@@ -867,7 +876,7 @@ int hg_encrypt_bn(hg_ctx* ctx, int key_id, const uint32_t* m_mag, const uint8_t*
 }
 
 int hg_encrypt_zero(hg_ctx* ctx, int key_id, const uint32_t* r, uint32_t* ct_out, size_t count) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     if (!r || !ct_out) fail(HG_ERR_INVALID, "null argument");
     HG_HOST_PROLOGUE
     const size_t rb = (size_t)k->kc.rlimbs * 4;
@@ -882,7 +891,7 @@ int hg_encrypt_zero(hg_ctx* ctx, int key_id, const uint32_t* r, uint32_t* ct_out
 }
 
 int hg_randomize(hg_ctx* ctx, int key_id, uint32_t* ct, const uint32_t* r, size_t count) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     if (!r || !ct) fail(HG_ERR_INVALID, "null argument");
     HG_HOST_PROLOGUE
     const size_t rb = (size_t)k->kc.rlimbs * 4;
@@ -898,7 +907,7 @@ int hg_randomize(hg_ctx* ctx, int key_id, uint32_t* ct, const uint32_t* r, size_
 }
 
 int hg_decrypt(hg_ctx* ctx, int key_id, const uint32_t* ct, int64_t* m_out, uint8_t* overflow, size_t count) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     if (!ct || !m_out) fail(HG_ERR_INVALID, "null argument");
     HG_HOST_PROLOGUE
     auto* dc = w.io[0].ensure<uint32_t>(count * cb);
@@ -914,7 +923,7 @@ int hg_decrypt(hg_ctx* ctx, int key_id, const uint32_t* ct, int64_t* m_out, uint
 }
 
 int hg_decrypt_bn(hg_ctx* ctx, int key_id, const uint32_t* ct, uint32_t* m_mag, uint8_t* m_neg, size_t count) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     if (!ct || !m_mag || !m_neg) fail(HG_ERR_INVALID, "null argument");
     HG_HOST_PROLOGUE
     const size_t pb = (size_t)k->S / 2 * 4;
@@ -931,7 +940,7 @@ int hg_decrypt_bn(hg_ctx* ctx, int key_id, const uint32_t* ct, uint32_t* m_mag, 
 }
 
 int hg_add(hg_ctx* ctx, int key_id, const uint32_t* a, const uint32_t* b, uint32_t* out, size_t count) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     if (!a || !b || !out) fail(HG_ERR_INVALID, "null argument");
     HG_HOST_PROLOGUE
     auto* da = w.io[0].ensure<uint32_t>(count * cb);
@@ -947,7 +956,7 @@ int hg_add(hg_ctx* ctx, int key_id, const uint32_t* a, const uint32_t* b, uint32
 
 static int add_plain_impl(hg_ctx* ctx, int key_id, const uint32_t* a, const int64_t* p, int neg, uint32_t* out,
                           size_t count) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     if (!a || !p || !out) fail(HG_ERR_INVALID, "null argument");
     HG_HOST_PROLOGUE
     auto* da = w.io[0].ensure<uint32_t>(count * cb);
@@ -970,7 +979,7 @@ int hg_sub_plain(hg_ctx* ctx, int key_id, const uint32_t* a, const int64_t* p, u
 }
 
 int hg_negate(hg_ctx* ctx, int key_id, const uint32_t* a, uint32_t* out, size_t count) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     if (!a || !out) fail(HG_ERR_INVALID, "null argument");
     HG_HOST_PROLOGUE
     auto* da = w.io[0].ensure<uint32_t>(count * cb);
@@ -983,7 +992,7 @@ int hg_negate(hg_ctx* ctx, int key_id, const uint32_t* a, uint32_t* out, size_t 
 }
 
 int hg_sub(hg_ctx* ctx, int key_id, const uint32_t* a, const uint32_t* b, uint32_t* out, size_t count) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     if (!a || !b || !out) fail(HG_ERR_INVALID, "null argument");
     HG_HOST_PROLOGUE
     auto* da = w.io[0].ensure<uint32_t>(count * cb);
@@ -1000,7 +1009,7 @@ int hg_sub(hg_ctx* ctx, int key_id, const uint32_t* a, const uint32_t* b, uint32
 }
 
 int hg_plain_sub(hg_ctx* ctx, int key_id, const int64_t* p, const uint32_t* a, uint32_t* out, size_t count) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     if (!a || !p || !out) fail(HG_ERR_INVALID, "null argument");
     HG_HOST_PROLOGUE
     auto* da = w.io[0].ensure<uint32_t>(count * cb);
@@ -1017,7 +1026,7 @@ int hg_plain_sub(hg_ctx* ctx, int key_id, const int64_t* p, const uint32_t* a, u
 }
 
 int hg_mul(hg_ctx* ctx, int key_id, const uint32_t* a, const int64_t* kk, uint32_t* out, size_t count) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     if (!a || !kk || !out) fail(HG_ERR_INVALID, "null argument");
     HG_HOST_PROLOGUE
     auto* da = w.io[0].ensure<uint32_t>(count * cb);
@@ -1033,7 +1042,7 @@ int hg_mul(hg_ctx* ctx, int key_id, const uint32_t* a, const int64_t* kk, uint32
 }
 
 int hg_sum(hg_ctx* ctx, int key_id, const uint32_t* a, size_t count, uint32_t* out) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     if (!a || !out) fail(HG_ERR_INVALID, "null argument");
     if (count == 0) fail(HG_ERR_INVALID, "you cannot sum an empty tensor");
     HG_HOST_PROLOGUE
@@ -1048,7 +1057,7 @@ int hg_sum(hg_ctx* ctx, int key_id, const uint32_t* a, size_t count, uint32_t* o
 }
 
 static int convert_impl(hg_ctx* ctx, int key_id, const uint32_t* in, uint32_t* out, size_t count, int to_mont) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     if (!in || !out) fail(HG_ERR_INVALID, "null argument");
     HG_HOST_PROLOGUE
     auto* da = w.io[0].ensure<uint32_t>(count * cb);
@@ -1090,7 +1099,7 @@ static Work& dev_work(hg_ctx* ctx, void* stream) {
 
 int hg_dev_encrypt(hg_ctx* ctx, int key_id, const int64_t* m, const uint32_t* r, uint32_t* ct_out, size_t count,
                    void* stream) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     HG_DEV_PROLOGUE
     core_encrypt(*k, w, hg::EncMode::kEncrypt, m, nullptr, nullptr, r, nullptr, ct_out, count);
     return HG_OK;
@@ -1099,7 +1108,7 @@ int hg_dev_encrypt(hg_ctx* ctx, int key_id, const int64_t* m, const uint32_t* r,
 
 int hg_dev_decrypt(hg_ctx* ctx, int key_id, const uint32_t* ct, int64_t* m_out, uint8_t* overflow, size_t count,
                    void* stream) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     HG_DEV_PROLOGUE
     core_decrypt(*k, w, ct, m_out, overflow, nullptr, nullptr, count);
     return HG_OK;
@@ -1108,7 +1117,7 @@ int hg_dev_decrypt(hg_ctx* ctx, int key_id, const uint32_t* ct, int64_t* m_out, 
 
 int hg_dev_add(hg_ctx* ctx, int key_id, const uint32_t* a, const uint32_t* b, uint32_t* out, size_t count,
                void* stream) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     HG_DEV_PROLOGUE
     cuda_check(hg::launch_add(k->S, k->kc, a, b, out, count, w.errp(), w.stream), "add launch");
     return HG_OK;
@@ -1117,7 +1126,7 @@ int hg_dev_add(hg_ctx* ctx, int key_id, const uint32_t* a, const uint32_t* b, ui
 
 int hg_dev_mul(hg_ctx* ctx, int key_id, const uint32_t* a, const int64_t* kk, uint32_t* out, size_t count,
                void* stream) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     HG_DEV_PROLOGUE
     core_mul(*k, w, a, kk, nullptr, out, count);
     return HG_OK;
@@ -1125,7 +1134,7 @@ int hg_dev_mul(hg_ctx* ctx, int key_id, const uint32_t* a, const int64_t* kk, ui
 }
 
 int hg_dev_encrypt_zero(hg_ctx* ctx, int key_id, const uint32_t* r, uint32_t* ct_out, size_t count, void* stream) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     HG_DEV_PROLOGUE
     core_encrypt(*k, w, hg::EncMode::kZero, nullptr, nullptr, nullptr, r, nullptr, ct_out, count);
     return HG_OK;
@@ -1133,7 +1142,7 @@ int hg_dev_encrypt_zero(hg_ctx* ctx, int key_id, const uint32_t* r, uint32_t* ct
 }
 
 int hg_dev_randomize(hg_ctx* ctx, int key_id, uint32_t* ct, const uint32_t* r, size_t count, void* stream) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     HG_DEV_PROLOGUE
     core_encrypt(*k, w, hg::EncMode::kRandomize, nullptr, nullptr, nullptr, r, ct, ct, count);
     return HG_OK;
@@ -1142,7 +1151,7 @@ int hg_dev_randomize(hg_ctx* ctx, int key_id, uint32_t* ct, const uint32_t* r, s
 
 int hg_dev_add_plain(hg_ctx* ctx, int key_id, const uint32_t* a, const int64_t* p, uint32_t* out, size_t count,
                      void* stream) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     HG_DEV_PROLOGUE
     cuda_check(hg::launch_add_plain(k->S, k->kc, a, p, 0, out, count, w.errp(), w.stream), "add_plain launch");
     return HG_OK;
@@ -1151,7 +1160,7 @@ int hg_dev_add_plain(hg_ctx* ctx, int key_id, const uint32_t* a, const int64_t* 
 
 int hg_dev_sub_plain(hg_ctx* ctx, int key_id, const uint32_t* a, const int64_t* p, uint32_t* out, size_t count,
                      void* stream) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     HG_DEV_PROLOGUE
     cuda_check(hg::launch_add_plain(k->S, k->kc, a, p, 1, out, count, w.errp(), w.stream), "add_plain launch");
     return HG_OK;
@@ -1166,7 +1175,7 @@ static void dev_negate_into(KeyRec& k, Work& w, const uint32_t* a, uint32_t* out
 }
 
 int hg_dev_negate(hg_ctx* ctx, int key_id, const uint32_t* a, uint32_t* out, size_t count, void* stream) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     HG_DEV_PROLOGUE
     dev_negate_into(*k, w, a, out, count);
     return HG_OK;
@@ -1175,7 +1184,7 @@ int hg_dev_negate(hg_ctx* ctx, int key_id, const uint32_t* a, uint32_t* out, siz
 
 int hg_dev_plain_sub(hg_ctx* ctx, int key_id, const int64_t* p, const uint32_t* a, uint32_t* out, size_t count,
                      void* stream) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     HG_DEV_PROLOGUE
     // evaluator.cc:82-84: Add(Negate(a), p)
     dev_negate_into(*k, w, a, out, count);
@@ -1186,7 +1195,7 @@ int hg_dev_plain_sub(hg_ctx* ctx, int key_id, const int64_t* p, const uint32_t* 
 
 int hg_dev_sub(hg_ctx* ctx, int key_id, const uint32_t* a, const uint32_t* b, uint32_t* out, size_t count,
                void* stream) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     HG_DEV_PROLOGUE
     // evaluator.cc:66-68: Add(a, Negate(b)); with out == a the inverse goes
     // through the context's staging buffer so a is not overwritten first
@@ -1199,7 +1208,7 @@ int hg_dev_sub(hg_ctx* ctx, int key_id, const uint32_t* a, const uint32_t* b, ui
 }
 
 int hg_dev_sum(hg_ctx* ctx, int key_id, const uint32_t* a, size_t count, uint32_t* out, void* stream) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     if (count == 0) fail(HG_ERR_INVALID, "you cannot sum an empty tensor");
     HG_DEV_PROLOGUE
     core_sum(*k, w, a, count, out);
@@ -1210,7 +1219,7 @@ int hg_dev_sum(hg_ctx* ctx, int key_id, const uint32_t* a, size_t count, uint32_
 
 int hg_bucket_sum(hg_ctx* ctx, int key_id, const uint32_t* x, size_t rows, size_t cols, const uint8_t* order_map,
                   size_t features, int bucket_num, int cumsum, uint32_t* out) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     if (!x || !order_map || !out) fail(HG_ERR_INVALID, "null argument");
     const size_t count = rows * cols;
     if (count == 0) fail(HG_ERR_INVALID, "you cannot sum an empty tensor");
@@ -1230,7 +1239,7 @@ int hg_bucket_sum(hg_ctx* ctx, int key_id, const uint32_t* x, size_t rows, size_
 
 int hg_dev_bucket_sum(hg_ctx* ctx, int key_id, const uint32_t* x, size_t rows, size_t cols, const uint8_t* order_map,
                       size_t features, int bucket_num, int cumsum, uint32_t* out, void* stream) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     const size_t count = rows * cols;
     if (count == 0) fail(HG_ERR_INVALID, "you cannot sum an empty tensor");
     HG_DEV_PROLOGUE
@@ -1241,7 +1250,7 @@ int hg_dev_bucket_sum(hg_ctx* ctx, int key_id, const uint32_t* x, size_t rows, s
 
 int hg_matmul(hg_ctx* ctx, int key_id, const uint32_t* x, size_t M, size_t K, const int64_t* y, size_t N,
               uint32_t* out) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     if (!x || !y || !out) fail(HG_ERR_INVALID, "null argument");
     const size_t count = M * K;
     if (count == 0 || N == 0) fail(HG_ERR_INVALID, "HEU does not support empty tensor currently");
@@ -1258,7 +1267,7 @@ int hg_matmul(hg_ctx* ctx, int key_id, const uint32_t* x, size_t M, size_t K, co
 
 int hg_dev_matmul(hg_ctx* ctx, int key_id, const uint32_t* x, size_t M, size_t K, const int64_t* y, size_t N,
                   uint32_t* out, void* stream) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     if (!y) fail(HG_ERR_INVALID, "null argument");
     const size_t count = M * K;
     if (count == 0 || N == 0) fail(HG_ERR_INVALID, "HEU does not support empty tensor currently");
@@ -1509,7 +1518,7 @@ void batch_enqueue(hg_batch& b, cudaStream_t st) {
 extern "C" {
 
 int hg_key_get_config(hg_ctx* ctx, int key_id, hg_key_config* out) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     if (!out) fail(HG_ERR_INVALID, "null argument");
     *out = current_config(*get_key(ctx, key_id));
     return HG_OK;
@@ -1517,7 +1526,7 @@ int hg_key_get_config(hg_ctx* ctx, int key_id, hg_key_config* out) {
 }
 
 int hg_key_set_config(hg_ctx* ctx, int key_id, const hg_key_config* cfg) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     if (!cfg) fail(HG_ERR_INVALID, "null argument");
     KeyRec* k = get_key(ctx, key_id);
     set_device(ctx);
@@ -1527,7 +1536,7 @@ int hg_key_set_config(hg_ctx* ctx, int key_id, const hg_key_config* cfg) {
 }
 
 int hg_autotune(hg_ctx* ctx, int key_id, size_t calib, hg_key_config* best, double* rates) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     KeyRec* k = get_key(ctx, key_id);
     set_device(ctx);
     const size_t n = calib ? calib : 65536;
@@ -1632,7 +1641,7 @@ int hg_autotune(hg_ctx* ctx, int key_id, size_t calib, hg_key_config* best, doub
 }
 
 int hg_batch_create(hg_ctx* ctx, hg_batch** out) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     if (!ctx || !out) fail(HG_ERR_INVALID, "null argument");
     auto b = std::make_unique<hg_batch>();
     b->ctx = ctx;
@@ -1642,7 +1651,7 @@ int hg_batch_create(hg_ctx* ctx, hg_batch** out) {
 }
 
 int hg_batch_destroy(hg_batch* b) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     if (b) {
       cudaSetDevice(b->ctx->device);
       cudaDeviceSynchronize();
@@ -1654,7 +1663,7 @@ int hg_batch_destroy(hg_batch* b) {
 
 int hg_batch_add(hg_batch* b, int key_id, int op, size_t count, const void* in0, const void* in1, void* out,
                  void* aux, int flags) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     if (!b) fail(HG_ERR_INVALID, "null batch");
     if (op < hg::kBatchEncrypt || op > hg::kBatchMul) fail(HG_ERR_INVALID, "unknown batch op");
     if (count == 0) return HG_OK;
@@ -1669,7 +1678,7 @@ int hg_batch_add(hg_batch* b, int key_id, int op, size_t count, const void* in0,
 }
 
 int hg_batch_clear(hg_batch* b) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     if (!b) fail(HG_ERR_INVALID, "null batch");
     b->jobs.clear();
     b->dirty = true;
@@ -1679,7 +1688,7 @@ int hg_batch_clear(hg_batch* b) {
 }
 
 int hg_batch_set_variant(hg_batch* b, int variant) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     if (!b || variant < 0 || variant > 1) fail(HG_ERR_INVALID, "variant must be 0 or 1");
     if (variant != b->variant) {
       b->variant = variant;
@@ -1691,7 +1700,7 @@ int hg_batch_set_variant(hg_batch* b, int variant) {
 }
 
 int hg_batch_run(hg_batch* b, void* stream, int use_graph) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     if (!b) fail(HG_ERR_INVALID, "null batch");
     set_device(b->ctx);
     cudaStream_t st = stream ? (cudaStream_t)stream : b->ctx->lanes[0]->stream;
@@ -1730,7 +1739,7 @@ int hg_batch_run(hg_batch* b, void* stream, int use_graph) {
 }
 
 int hg_batch_wait(hg_batch* b, void* stream) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     if (!b) fail(HG_ERR_INVALID, "null batch");
     set_device(b->ctx);
     cudaStream_t st = stream ? (cudaStream_t)stream : b->ctx->lanes[0]->stream;
@@ -1744,7 +1753,7 @@ int hg_batch_wait(hg_batch* b, void* stream) {
 
 
 int hg_server_create(hg_ctx* ctx, const hg_server_config* cfg, hg_server** out) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     if (!ctx || !out) fail(HG_ERR_INVALID, "null argument");
     set_device(ctx);
     auto s = std::make_unique<hg_server>();
@@ -1821,7 +1830,7 @@ int hg_server_create(hg_ctx* ctx, const hg_server_config* cfg, hg_server** out) 
 }
 
 int hg_server_destroy(hg_server* s) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     if (!s) return HG_OK;
     {
       std::lock_guard<std::mutex> lk(s->mu);
@@ -1841,7 +1850,7 @@ int hg_server_destroy(hg_server* s) {
 }
 
 int hg_server_store(hg_server* s, int key_id, const uint32_t* host_ct, size_t count, uint64_t* handle) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     if (!s || !host_ct || !handle || count == 0) fail(HG_ERR_INVALID, "null argument");
     KeyRec* k = get_key(s->ctx, key_id);
     set_device(s->ctx);
@@ -1858,7 +1867,7 @@ int hg_server_store(hg_server* s, int key_id, const uint32_t* host_ct, size_t co
 }
 
 int hg_server_release(hg_server* s, uint64_t handle) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     if (!s) fail(HG_ERR_INVALID, "null server");
     std::unique_lock<std::mutex> lk(s->mu);
     // no request in flight may still read it
@@ -1869,7 +1878,7 @@ int hg_server_release(hg_server* s, uint64_t handle) {
 }
 
 int hg_server_submit(hg_server* s, const hg_request* req, uint64_t* ticket) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     if (!s || !req || !ticket) fail(HG_ERR_INVALID, "null argument");
     if (req->op < hg::kBatchEncrypt || req->op > kOpSum) fail(HG_ERR_INVALID, "unknown request op");
     if (req->count == 0) fail(HG_ERR_INVALID, "empty request");
@@ -1903,7 +1912,7 @@ int hg_server_submit(hg_server* s, const hg_request* req, uint64_t* ticket) {
 
 int hg_server_wait(hg_server* s, uint64_t ticket, double* latency_s) {
   int status = HG_OK;
-  const int rc = guarded([&] {
+  const int rc = guarded(__func__, [&] {
     if (!s) fail(HG_ERR_INVALID, "null server");
     std::unique_lock<std::mutex> lk(s->mu);
     auto it = s->reqs.find(ticket);
@@ -1921,7 +1930,7 @@ int hg_server_wait(hg_server* s, uint64_t ticket, double* latency_s) {
 }
 
 int hg_server_stats(hg_server* s, uint64_t* completed, uint64_t* batches, size_t* inflight_bytes, size_t* pending) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     if (!s) fail(HG_ERR_INVALID, "null server");
     std::lock_guard<std::mutex> lk(s->mu);
     if (completed) *completed = s->completed;
@@ -1934,7 +1943,7 @@ int hg_server_stats(hg_server* s, uint64_t* completed, uint64_t* batches, size_t
 
 int hg_probe_serve_load(hg_server* s, const hg_load_spec* spec, double* latencies, int* ops, uint64_t* lens,
                         double* wall_s) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     if (!s || !spec || !latencies) fail(HG_ERR_INVALID, "null argument");
     std::mt19937_64 rng(spec->seed);
     std::exponential_distribution<double> gap(spec->rate);
@@ -1997,7 +2006,7 @@ int hg_probe_launch_count(uint64_t* out) {
 }
 
 int hg_dev_check(hg_ctx* ctx) {
-  return guarded([&] {
+  return guarded(__func__, [&] {
     if (!ctx) fail(HG_ERR_INVALID, "null context");
     set_device(ctx);
     uint32_t bits = 0;
