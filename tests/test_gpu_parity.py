@@ -407,7 +407,8 @@ def test_injected_allocation_failure_keeps_the_context_usable():
         capi.check(lib.hg_probe_set_alloc_limit(0, ctypes.byref(held)))
         n = 4096
         m = np.arange(n, dtype=np.int64) - n // 2
-        r = np.ones((n, key.r_limbs), np.uint32)
+        r = np.zeros((n, key.r_limbs), np.uint32)
+        r[:, 0] = 1  # r = 1
         try:
             capi.check(lib.hg_probe_set_alloc_limit(held.value + 4096, None))
             with pytest.raises(hg.HgError) as ei:
