@@ -45,6 +45,8 @@ SIGNATURES = {
     "hg_keygen": [_U32, _U64, _P, _P, _P, _P],
     "hg_key_load": [_P, _U32, _P, _P, _P, _P, _I, ctypes.POINTER(_I)],
     "hg_key_free": [_P, _I],
+    "hg_ou_keygen": [_U32, _U64, _P, _P, _P, _P, _P, _P, _P, ctypes.POINTER(_I)],
+    "hg_ou_key_load": [_P, _U32, _P, _P, _P, _I, _P, _P, _P, _P, _I, ctypes.POINTER(_I)],
     "hg_key_shape": [_P, _I, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I)],
     "hg_encrypt": [_P, _I, _P, _P, _P, _SZ],
     "hg_encrypt_bn": [_P, _I, _P, _P, _P, _P, _SZ],

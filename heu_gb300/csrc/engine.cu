@@ -161,6 +161,15 @@ struct KeyRec {
   hg::SecConst sc{};
   int grid_mul = 0, grid_dec = 0;
   int wm = 4;  // scalar-mul window
+  // Okamoto-Uchiyama keys (scheme 1): kc is over n with the H table; kcG /
+  // kcGi hold the G and G^-1 tables; oc the decryption constants
+  int scheme = 0;
+  hg::KeyConst kcG{}, kcGi{};
+  DevBuf tableG, tableGi, oconsts, oprog;
+  hg::OuConst oc{};
+  int pt_limbs = 0, max_pt_bits = 0;
+  int grid_oudec = 0, upb_oudec = 0;
+  const uint32_t* d_maxpt = nullptr;  // max plaintext (pt_limbs), on the device
 };
 
 // Asynchronous inversion of the root of a product tree: the host function
@@ -228,6 +237,7 @@ struct Work {
   TreeBufs inv;
   DevBuf seg_cnt, seg_offs[3], seg_cursor, seg_idx, seg_nch, seg_part[2];
   DevBuf mm_tables, mm_masks, mm_prod;
+  DevBuf ou_e[2];
   DevBuf err;
   PinBuf pin_root, pin_err, pin_z;
   InvTask task;
@@ -313,15 +323,65 @@ void d2h(void* h, const void* d, size_t bytes, Work& w) {
 // ---------------------------------------------------------------------------
 size_t ct_bytes(const KeyRec& k) { return (size_t)k.S * 4; }
 
+// OU: out = [ct_in or 1] * G^(m+) * (G^-1)^(m-) [* H^r]  (encryptor.cc:92-117,
+// evaluator.cc:35-50), as three passes of the fixed-base kernel.
+void ou_plain_pow(KeyRec& k, Work& w, const int64_t* m, int negate, const uint32_t* m_mag, const uint8_t* m_neg,
+                  const uint32_t* r, const uint32_t* ct_in, uint32_t* out, size_t count) {
+  const int el = m ? 2 : k.pt_limbs;  // exponent limbs
+  uint32_t* ep = w.ou_e[0].ensure<uint32_t>(count * el * 4);
+  uint32_t* en = w.ou_e[1].ensure<uint32_t>(count * el * 4);
+  if (m)
+    cuda_check(hg::launch_ou_split_i64(m, negate, ep, en, count, w.stream), "OU split");
+  else
+    cuda_check(hg::launch_ou_split_mag(m_mag, m_neg, el, k.d_maxpt, ep, en, count, w.errp(), w.stream),
+               "OU split");
+  hg::KeyConst g = k.kcG, gi = k.kcGi;
+  g.rlimbs = gi.rlimbs = el;
+  g.rbits = gi.rbits = m ? 64 : k.max_pt_bits;
+  g.npos = gi.npos = (g.rbits + g.w - 1) / g.w;
+  cuda_check(hg::launch_encrypt(k.S, g, ct_in ? hg::EncMode::kRandomize : hg::EncMode::kZero, nullptr, nullptr,
+                                nullptr, ep, ct_in, out, count, w.errp(), 0, w.stream),
+             "OU G pass");
+  cuda_check(hg::launch_encrypt(k.S, gi, hg::EncMode::kRandomize, nullptr, nullptr, nullptr, en, out, out, count,
+                                w.errp(), 0, w.stream),
+             "OU G^-1 pass");
+  if (r)
+    cuda_check(hg::launch_encrypt(k.S, k.kc, hg::EncMode::kRandomize, nullptr, nullptr, nullptr, r, out, out, count,
+                                  w.errp(), 0, w.stream),
+               "OU H pass");
+}
+
 void core_encrypt(KeyRec& k, Work& w, hg::EncMode mode, const int64_t* m, const uint32_t* m_mag,
                   const uint8_t* m_neg, const uint32_t* r, const uint32_t* ct_in, uint32_t* out, size_t count) {
+  if (k.scheme == 1 && mode == hg::EncMode::kEncrypt) {
+    ou_plain_pow(k, w, m, 0, m_mag, m_neg, r, nullptr, out, count);
+    return;
+  }
   cuda_check(hg::launch_encrypt(k.S, k.kc, mode, m, m_mag, m_neg, r, ct_in, out, count, w.errp(), 0, w.stream),
              "encrypt launch");
+}
+
+// Add(ct, pt) / Sub(ct, pt) with int64 plaintexts, per scheme.
+void core_add_plain(KeyRec& k, Work& w, const uint32_t* a, const int64_t* p, int neg, uint32_t* out, size_t count) {
+  if (k.scheme == 1) {
+    ou_plain_pow(k, w, p, neg, nullptr, nullptr, nullptr, a, out, count);
+    return;
+  }
+  cuda_check(hg::launch_add_plain(k.S, k.kc, a, p, neg, out, count, w.errp(), w.stream), "add_plain launch");
 }
 
 void core_decrypt(KeyRec& k, Work& w, const uint32_t* ct, int64_t* m, uint8_t* ovf, uint32_t* mag, uint8_t* neg,
                   size_t count) {
   if (!k.secret) fail(HG_ERR_NO_SECRET, "key has no secret part");
+  if (k.scheme == 1) {
+    const size_t ntab = (size_t)1 << (k.oc.wd - 1);
+    const size_t units = (size_t)k.grid_oudec * k.upb_oudec;
+    uint32_t* scratch = w.scratch.ensure<uint32_t>(units * ntab * k.oc.Sp * 4);
+    cuda_check(hg::launch_ou_decrypt(k.S, k.kc, k.oc, ct, count, m, ovf, mag, neg, scratch, w.errp(), k.grid_oudec,
+                                     w.stream),
+               "OU decrypt launch");
+    return;
+  }
   const size_t ntab = (size_t)1 << (k.sc.wd - 1);
   const size_t units = (size_t)k.grid_dec * hg::units_per_block_decrypt(k.Sp, k.sc.variant);
   uint32_t* scratch = w.scratch.ensure<uint32_t>(units * 2 * ntab * k.Sp * 4);
@@ -663,6 +723,155 @@ int load_key(hg_ctx* ctx, uint32_t key_bits, const uint32_t* n_l, const uint32_t
   return id;
 }
 
+// Fixed-base table of `base_mont` powers over the modulus of `t` (npos x
+// (2^w - 1) entries, Montgomery form), the layout k_encrypt reads.
+void build_fixed_base(int S, hg::KeyConst& t, DevBuf& buf, const uint32_t* base_mont, int exp_bits, int window) {
+  t.w = window;
+  t.rbits = exp_bits;
+  t.npos = (exp_bits + window - 1) / window;
+  const size_t ent = ((size_t)1 << window) - 1;
+  t.table = buf.ensure<uint32_t>((size_t)t.npos * ent * S * 4);
+  DevBuf bases;
+  uint32_t* b = bases.ensure<uint32_t>((size_t)t.npos * S * 4);
+  cuda_check(hg::launch_table_bases(S, t, base_mont, b, nullptr), "table bases");
+  cuda_check(hg::launch_table_level(S, t, const_cast<uint32_t*>(t.table), b, -1, nullptr), "table level");
+  for (int lv = 0; lv < window; ++lv)
+    cuda_check(hg::launch_table_level(S, t, const_cast<uint32_t*>(t.table), b, lv, nullptr), "table level");
+  cuda_check(cudaDeviceSynchronize(), "table build");
+}
+
+int ou_random_bits(size_t n_bits) {  // ou/encryptor.cc:12-20, public_key.h:27-31
+  return n_bits >= 2560 ? 128 : n_bits >= 1536 ? 110 : 80;
+}
+
+void ou_sizes(uint32_t key_bits, int* S, int* Sp) {
+  if (key_bits == 1024) {
+    *S = 64;
+    *Sp = 32;
+  } else if (key_bits == 2048) {
+    *S = 128;
+    *Sp = 64;
+  } else if (key_bits == 3072) {
+    *S = 128;
+    *Sp = 96;
+  } else {
+    fail(HG_ERR_UNSUPPORTED, "OU keys of 1024, 2048 or 3072 bits");
+  }
+}
+
+// Okamoto-Uchiyama key (ou/public_key.cc:28-41, secret_key.h): tables for
+// H (encryption randomness), G and G^-1 (plaintexts); CRT-free decryption
+// constants mod p^2.
+int load_ou_key(hg_ctx* ctx, uint32_t key_bits, const uint32_t* n_l, const uint32_t* G_l, const uint32_t* H_l,
+                int max_pt_bits, const uint32_t* p_l, const uint32_t* q_l, const uint32_t* t_l,
+                const uint32_t* gpinv_l, int window) {
+  int S = 0, Sp = 0;
+  ou_sizes(key_bits, &S, &Sp);
+  const int Hh = Sp / 2;
+  auto k = std::make_unique<KeyRec>();
+  k->scheme = 1;
+  k->key_bits = (int)key_bits;
+  k->S = S;
+  k->Sp = Sp;
+  k->H = Hh;
+  k->pt_limbs = Hh;
+  k->n = BN::from_limbs(n_l, S);
+  k->N = k->n;
+  if (!k->n.is_odd() || k->n.bitlen() < 64) fail(HG_ERR_INVALID, "n must be odd");
+  if (max_pt_bits < 2 || max_pt_bits > 32 * Hh) fail(HG_ERR_INVALID, "max plaintext bits out of range");
+  k->max_pt_bits = max_pt_bits + 1;  // |m| <= 2^max_pt_bits has max_pt_bits + 1 bits
+  const BN G = BN::from_limbs(G_l, S), Hb = BN::from_limbs(H_l, S);
+  if (G >= k->N || Hb >= k->N) fail(HG_ERR_INVALID, "G and H must be < n");
+  if (BN::gcd(G, k->N) != BN(1)) fail(HG_ERR_INVALID, "G is not invertible mod n");
+  const BN Gi = BN::invmod(G, k->N);
+  const BN R = BN(1).shl(32 * (size_t)S);
+  const BN R1 = R % k->N, R2 = (R1 * R1) % k->N, R3 = (R2 * R1) % k->N;
+  const BN maxpt = BN(1).shl((size_t)max_pt_bits);
+  // N R1 R2 R3 nR2(0) Hm Gm Gim zeros(S) maxpt(Hh)
+  std::vector<uint32_t> hc(9 * (size_t)S + Hh, 0u);
+  auto put = [&](size_t at, const BN& v, size_t limbs) { v.to_limbs(hc.data() + at, limbs); };
+  put(0, k->N, S);
+  put(S, R1, S);
+  put(2 * S, R2, S);
+  put(3 * S, R3, S);
+  put(5 * S, (Hb * R1) % k->N, S);
+  put(6 * S, (G * R1) % k->N, S);
+  put(7 * S, (Gi * R1) % k->N, S);
+  put(9 * S, maxpt, Hh);
+  uint32_t* dc = k->consts.ensure<uint32_t>(hc.size() * 4);
+  cuda_check(cudaMemcpy(dc, hc.data(), hc.size() * 4, cudaMemcpyHostToDevice), "upload consts");
+  auto& kc = k->kc;
+  kc.N = dc;
+  kc.R1 = dc + S;
+  kc.R2 = dc + 2 * S;
+  kc.R3 = dc + 3 * S;
+  kc.nR2 = dc + 4 * S;
+  kc.n = dc + 8 * S;
+  kc.nhalf = dc + 8 * S;
+  kc.np = neg_inv32(k->N.d[0]);
+  kc.S = S;
+  kc.variant = 0;
+  k->d_maxpt = dc + 9 * S;
+  const int w = window > 0 ? window : 12;
+  if (w > 20) fail(HG_ERR_INVALID, "table window must be <= 20");
+  k->kcG = kc;
+  k->kcGi = kc;
+  // H^r with r < 2^128 (the table covers kRandomBits3072, public_key.cc:38-39)
+  build_fixed_base(S, kc, k->table, dc + 5 * S, 128, w);
+  kc.rbits = ou_random_bits(k->n.bitlen());
+  kc.npos = (kc.rbits + w - 1) / w;
+  kc.rlimbs = 4;
+  build_fixed_base(S, k->kcG, k->tableG, dc + 6 * S, k->max_pt_bits, w);
+  build_fixed_base(S, k->kcGi, k->tableGi, dc + 7 * S, k->max_pt_bits, w);
+  k->grid_mul = hg::resident_blocks_mul(S, 0);
+  if (p_l && q_l && t_l && gpinv_l) {
+    k->p = BN::from_limbs(p_l, S / 2);
+    k->q = BN::from_limbs(q_l, S / 2);
+    const BN t = BN::from_limbs(t_l, S / 2), gpinv = BN::from_limbs(gpinv_l, S / 2);
+    const BN p2 = k->p * k->p;
+    if (p2 * k->q != k->n) fail(HG_ERR_INVALID, "pk and sk are not paired: p^2 * q != n");
+    if (p2.bitlen() > 32 * (size_t)Sp || k->p.bitlen() > 32 * (size_t)Hh) fail(HG_ERR_INVALID, "p too large");
+    k->secret = true;
+    const BN Rp = BN(1).shl(32 * (size_t)Sp), Rh = BN(1).shl(32 * (size_t)Hh);
+    const BN Rp1 = Rp % p2;
+    const BN Kfix = (((Rp1 * Rp1) % p2) * Rp1 % p2) * BN::invmod(R % p2, p2) % p2;
+    // p2 Kfix (Sp) | p gpR pinv phalf (Hh)
+    std::vector<uint32_t> hs2(2 * (size_t)Sp + 4 * (size_t)Hh, 0u);
+    auto put2 = [&](size_t at, const BN& v, size_t limbs) { v.to_limbs(hs2.data() + at, limbs); };
+    put2(0, p2, Sp);
+    put2(Sp, Kfix, Sp);
+    const size_t o = 2 * (size_t)Sp;
+    put2(o, k->p, Hh);
+    put2(o + Hh, (gpinv * (Rh % k->p)) % k->p, Hh);
+    put2(o + 2 * Hh, BN::invmod(k->p, Rh), Hh);
+    put2(o + 3 * Hh, k->p.shr(1), Hh);
+    uint32_t* ds = k->oconsts.ensure<uint32_t>(hs2.size() * 4);
+    cuda_check(cudaMemcpy(ds, hs2.data(), hs2.size() * 4, cudaMemcpyHostToDevice), "upload secret consts");
+    auto& oc = k->oc;
+    oc.Sp = Sp;
+    oc.P2 = ds;
+    oc.Kfix = ds + Sp;
+    oc.P = ds + o;
+    oc.gpR = ds + o + Hh;
+    oc.pinv = ds + o + 2 * Hh;
+    oc.phalf = ds + o + 3 * Hh;
+    oc.np2 = neg_inv32(p2.d[0]);
+    oc.np1 = neg_inv32(k->p.d[0]);
+    oc.wd = 5;
+    std::vector<uint16_t> prog;
+    build_prog(t, oc.wd, &oc.start, &prog);
+    oc.prog_len = (int)prog.size();
+    uint16_t* dp = k->oprog.ensure<uint16_t>(std::max<size_t>(prog.size(), 1) * 2);
+    if (!prog.empty()) cuda_check(cudaMemcpy(dp, prog.data(), prog.size() * 2, cudaMemcpyHostToDevice), "prog");
+    oc.prog = dp;
+    cuda_check(hg::ou_decrypt_geometry(S, Sp, &k->grid_oudec, &k->upb_oudec), "OU decrypt geometry");
+  }
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  const int id = ctx->next_key++;
+  ctx->keys[id] = std::move(k);
+  return id;
+}
+
 // key generation (key_generator.cc:26-60) from a seeded stream
 std::vector<uint32_t> small_primes() {
   std::vector<uint32_t> out;
@@ -806,6 +1015,81 @@ int hg_key_load(hg_ctx* ctx, uint32_t key_bits, const uint32_t* n, const uint32_
   });
 }
 
+int hg_ou_keygen(uint32_t key_bits, uint64_t seed, uint32_t* n_out, uint32_t* G_out, uint32_t* H_out,
+                 uint32_t* p_out, uint32_t* q_out, uint32_t* t_out, uint32_t* gpinv_out, int* max_pt_bits) {
+  return guarded(__func__, [&] {
+    int S = 0, Sp = 0;
+    ou_sizes(key_bits, &S, &Sp);
+    hg::Xoshiro prg(seed);
+    const auto sp = small_primes();
+    const size_t secret = (key_bits + 2) / 3;
+    const size_t pf = key_bits >= 3072 ? 256 : key_bits >= 2048 ? 224 : 160;
+    if (pf * 2 > secret) fail(HG_ERR_INVALID, "Key size too small");
+    auto rand_prime = [&](size_t bits) {
+      while (true) {
+        BN c = prg.randbits(bits);
+        c.d.resize((bits + 31) / 32, 0);
+        c.d[(bits - 1) / 32] |= 1u << ((bits - 1) % 32);
+        c.d[0] |= 1u;
+        c.trim();
+        if (is_probable_prime(c, sp)) return c;
+      }
+    };
+    const size_t ub = secret - pf + 2;
+    BN t, u, p;
+    while (true) {
+      t = rand_prime(pf);
+      u = prg.randbits(ub);
+      u.d.resize((ub + 31) / 32, 0);
+      u.d[(ub - 1) / 32] |= 1u << ((ub - 1) % 32);
+      u.trim();
+      p = t * u + BN(1);
+      if (is_probable_prime(p, sp)) break;
+    }
+    const BN q = rand_prime(secret + 1);
+    const BN p2 = p * p, n = p2 * q;
+    BN g, gp;
+    while (true) {
+      while (true) {
+        g = prg.below(n);
+        if (BN::gcd(g, p) == BN(1)) break;
+      }
+      gp = hg::HostMont(p2).pow(g % p2, p - BN(1));
+      if (hg::HostMont(p2).pow(gp, p) == BN(1)) break;
+    }
+    const BN gpinv = BN::invmod((gp - BN(1)) / p, p);
+    BN g2;
+    while (true) {
+      g2 = prg.below(n);
+      if (!(g2 % p).is_zero()) break;
+    }
+    hg::HostMont mn(n);
+    const BN G = mn.pow(g, u), Hb = mn.pow(g2, n * u);
+    if (n_out) n.to_limbs(n_out, S);
+    if (G_out) G.to_limbs(G_out, S);
+    if (H_out) Hb.to_limbs(H_out, S);
+    if (p_out) p.to_limbs(p_out, S / 2);
+    if (q_out) q.to_limbs(q_out, S / 2);
+    if (t_out) t.to_limbs(t_out, S / 2);
+    if (gpinv_out) gpinv.to_limbs(gpinv_out, S / 2);
+    if (max_pt_bits) *max_pt_bits = (int)p.shr(1).bitlen() - 1;
+    return HG_OK;
+  });
+}
+
+int hg_ou_key_load(hg_ctx* ctx, uint32_t key_bits, const uint32_t* n, const uint32_t* G, const uint32_t* H,
+                   int max_pt_bits, const uint32_t* p, const uint32_t* q, const uint32_t* t, const uint32_t* gp_inv,
+                   int table_window, int* key_id) {
+  return guarded(__func__, [&] {
+    if (!ctx || !n || !G || !H || !key_id) fail(HG_ERR_INVALID, "null argument");
+    const bool any = p || q || t || gp_inv, all = p && q && t && gp_inv;
+    if (any && !all) fail(HG_ERR_INVALID, "give all of p, q, t, gp_inv or none");
+    set_device(ctx);
+    *key_id = load_ou_key(ctx, key_bits, n, G, H, max_pt_bits, p, q, t, gp_inv, table_window);
+    return HG_OK;
+  });
+}
+
 int hg_key_free(hg_ctx* ctx, int key_id) {
   return guarded(__func__, [&] {
     if (!ctx) fail(HG_ERR_INVALID, "null context");
@@ -822,7 +1106,7 @@ int hg_key_shape(hg_ctx* ctx, int key_id, int* ct_limbs, int* r_limbs, int* pt_l
     KeyRec* k = get_key(ctx, key_id);
     if (ct_limbs) *ct_limbs = k->S;
     if (r_limbs) *r_limbs = k->kc.rlimbs;
-    if (pt_limbs) *pt_limbs = k->S / 2;
+    if (pt_limbs) *pt_limbs = k->scheme == 1 ? k->pt_limbs : k->S / 2;
     return HG_OK;
   });
 }
@@ -860,7 +1144,7 @@ int hg_encrypt_bn(hg_ctx* ctx, int key_id, const uint32_t* m_mag, const uint8_t*
   return guarded(__func__, [&] {
     if (!m_mag || !m_neg || !r || !ct_out) fail(HG_ERR_INVALID, "null argument");
     HG_HOST_PROLOGUE
-    const size_t rb = (size_t)k->kc.rlimbs * 4, pb = (size_t)k->S / 2 * 4;
+    const size_t rb = (size_t)k->kc.rlimbs * 4, pb = (size_t)(k->scheme == 1 ? k->pt_limbs : k->S / 2) * 4;
     auto* dmag = w.io[0].ensure<uint32_t>(count * pb);
     auto* dneg = w.io[3].ensure<uint8_t>(count);
     auto* dr = w.io[1].ensure<uint32_t>(count * rb);
@@ -926,7 +1210,7 @@ int hg_decrypt_bn(hg_ctx* ctx, int key_id, const uint32_t* ct, uint32_t* m_mag, 
   return guarded(__func__, [&] {
     if (!ct || !m_mag || !m_neg) fail(HG_ERR_INVALID, "null argument");
     HG_HOST_PROLOGUE
-    const size_t pb = (size_t)k->S / 2 * 4;
+    const size_t pb = (size_t)(k->scheme == 1 ? k->pt_limbs : k->S / 2) * 4;
     auto* dc = w.io[0].ensure<uint32_t>(count * cb);
     auto* dmag = w.io[1].ensure<uint32_t>(count * pb);
     auto* dneg = w.io[2].ensure<uint8_t>(count);
@@ -963,7 +1247,7 @@ static int add_plain_impl(hg_ctx* ctx, int key_id, const uint32_t* a, const int6
     auto* dp = w.io[1].ensure<int64_t>(count * 8);
     h2d(da, a, count * cb, w);
     h2d(dp, p, count * 8, w);
-    cuda_check(hg::launch_add_plain(k->S, k->kc, da, dp, neg, da, count, w.errp(), w.stream), "add_plain launch");
+    core_add_plain(*k, w, da, dp, neg, da, count);
     d2h(out, da, count * cb, w);
     finish(w);
     return HG_OK;
@@ -1018,7 +1302,7 @@ int hg_plain_sub(hg_ctx* ctx, int key_id, const int64_t* p, const uint32_t* a, u
     h2d(dp, p, count * 8, w);
     // evaluator.cc:82-84: Add(Negate(a), p)
     core_inverse(*k, w, da, nullptr, da, count);
-    cuda_check(hg::launch_add_plain(k->S, k->kc, da, dp, 0, da, count, w.errp(), w.stream), "add_plain launch");
+    core_add_plain(*k, w, da, dp, 0, da, count);
     d2h(out, da, count * cb, w);
     finish(w);
     return HG_OK;
@@ -1153,7 +1437,7 @@ int hg_dev_add_plain(hg_ctx* ctx, int key_id, const uint32_t* a, const int64_t* 
                      void* stream) {
   return guarded(__func__, [&] {
     HG_DEV_PROLOGUE
-    cuda_check(hg::launch_add_plain(k->S, k->kc, a, p, 0, out, count, w.errp(), w.stream), "add_plain launch");
+    core_add_plain(*k, w, a, p, 0, out, count);
     return HG_OK;
   });
 }
@@ -1162,7 +1446,7 @@ int hg_dev_sub_plain(hg_ctx* ctx, int key_id, const uint32_t* a, const int64_t* 
                      void* stream) {
   return guarded(__func__, [&] {
     HG_DEV_PROLOGUE
-    cuda_check(hg::launch_add_plain(k->S, k->kc, a, p, 1, out, count, w.errp(), w.stream), "add_plain launch");
+    core_add_plain(*k, w, a, p, 1, out, count);
     return HG_OK;
   });
 }
@@ -1188,7 +1472,7 @@ int hg_dev_plain_sub(hg_ctx* ctx, int key_id, const int64_t* p, const uint32_t* 
     HG_DEV_PROLOGUE
     // evaluator.cc:82-84: Add(Negate(a), p)
     dev_negate_into(*k, w, a, out, count);
-    cuda_check(hg::launch_add_plain(k->S, k->kc, out, p, 0, out, count, w.errp(), w.stream), "add_plain launch");
+    core_add_plain(*k, w, out, p, 0, out, count);
     return HG_OK;
   });
 }
@@ -1529,6 +1813,7 @@ int hg_key_set_config(hg_ctx* ctx, int key_id, const hg_key_config* cfg) {
   return guarded(__func__, [&] {
     if (!cfg) fail(HG_ERR_INVALID, "null argument");
     KeyRec* k = get_key(ctx, key_id);
+    if (k->scheme != 0) fail(HG_ERR_UNSUPPORTED, "this call serves ZPaillier keys only");
     set_device(ctx);
     apply_config(*k, *cfg);
     return HG_OK;
@@ -1538,6 +1823,7 @@ int hg_key_set_config(hg_ctx* ctx, int key_id, const hg_key_config* cfg) {
 int hg_autotune(hg_ctx* ctx, int key_id, size_t calib, hg_key_config* best, double* rates) {
   return guarded(__func__, [&] {
     KeyRec* k = get_key(ctx, key_id);
+    if (k->scheme != 0) fail(HG_ERR_UNSUPPORTED, "this call serves ZPaillier keys only");
     set_device(ctx);
     const size_t n = calib ? calib : 65536;
     LaneGuard lane(ctx);
@@ -1669,7 +1955,7 @@ int hg_batch_add(hg_batch* b, int key_id, int op, size_t count, const void* in0,
     if (count == 0) return HG_OK;
     if (!in0 || !out || (op != hg::kBatchDecrypt && !in1)) fail(HG_ERR_INVALID, "null job pointer");
     if (count >= (1ull << 31)) fail(HG_ERR_INVALID, "job too large");
-    (void)get_key(b->ctx, key_id);
+    if (get_key(b->ctx, key_id)->scheme != 0) fail(HG_ERR_UNSUPPORTED, "batches serve ZPaillier keys only");
     b->jobs.push_back({key_id, op, flags, count, in0, in1, out, aux});
     b->dirty = true;
     b->drop_graph();
@@ -1797,6 +2083,7 @@ int hg_server_create(hg_ctx* ctx, const hg_server_config* cfg, hg_server** out) 
       std::lock_guard<std::mutex> lk(ctx->mu);
       for (auto& kv : ctx->keys) {
         const KeyRec& k = *kv.second;
+        if (k.scheme != 0) continue;  // the server serves ZPaillier keys only
         warp_words = std::max(warp_words, (size_t)(32 / hg::tpi_for(k.S, c.variant)) * ((size_t)1 << (k.wm - 1)) * k.S);
         if (k.secret)
           warp_words = std::max(warp_words, (size_t)(32 / (2 * hg::tp_for(k.Sp, c.variant))) * 2 *
@@ -1853,6 +2140,7 @@ int hg_server_store(hg_server* s, int key_id, const uint32_t* host_ct, size_t co
   return guarded(__func__, [&] {
     if (!s || !host_ct || !handle || count == 0) fail(HG_ERR_INVALID, "null argument");
     KeyRec* k = get_key(s->ctx, key_id);
+    if (k->scheme != 0) fail(HG_ERR_UNSUPPORTED, "this call serves ZPaillier keys only");
     set_device(s->ctx);
     auto r = std::make_unique<Resident>();
     r->key_id = key_id;
@@ -1884,6 +2172,7 @@ int hg_server_submit(hg_server* s, const hg_request* req, uint64_t* ticket) {
     if (req->count == 0) fail(HG_ERR_INVALID, "empty request");
     if (!req->out) fail(HG_ERR_INVALID, "request without an output buffer");
     KeyRec* k = get_key(s->ctx, req->key_id);
+    if (k->scheme != 0) fail(HG_ERR_UNSUPPORTED, "this call serves ZPaillier keys only");
     if (req->op == hg::kBatchDecrypt && !k->secret) fail(HG_ERR_NO_SECRET, "decrypt request on a public key");
     if ((req->op == hg::kBatchEncrypt || req->op == hg::kBatchMul) && (!req->in0 && !req->h0))
       fail(HG_ERR_INVALID, "request without input");

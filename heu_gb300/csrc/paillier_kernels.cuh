@@ -51,6 +51,23 @@ struct SecConst {
   int variant;              // (threads per unit side, limbs per thread) variant
 };
 
+// Okamoto-Uchiyama secret constants (ou/secret_key.h; decryptor.cc:27-45).
+struct OuConst {
+  const uint32_t* P2;     // p^2                                 (Sp limbs)
+  const uint32_t* Kfix;   // R_p^3 * R_n^-1 mod p^2              (Sp limbs)
+  const uint32_t* P;      // p                                   (Sp/2 limbs)
+  const uint32_t* gpR;    // gp_inv * 2^(16*Sp) mod p            (Sp/2 limbs)
+  const uint32_t* pinv;   // p^-1 mod 2^(16*Sp)                  (Sp/2 limbs)
+  const uint32_t* phalf;  // p >> 1                              (Sp/2 limbs)
+  const uint16_t* prog;   // sliding-window program of the exponent t
+  uint32_t np2;           // -(p^2)^-1 mod 2^32
+  uint32_t np1;           // -p^-1 mod 2^32
+  int start;              // first window's table index
+  int prog_len;
+  int wd;                 // window bits
+  int Sp;                 // 32-bit limbs of the p^2 arithmetic
+};
+
 // Exponent-program opcodes (one Montgomery multiplication per step).
 constexpr uint16_t kOpSquare = 0xFFFFu;
 constexpr uint16_t kOpNop = 0xFFFEu;
@@ -71,6 +88,17 @@ cudaError_t launch_mul(int S, const KeyConst& kc, const uint32_t* a, const int64
 cudaError_t launch_decrypt(int Sp, const KeyConst& kc, const SecConst& sc, const uint32_t* ct, size_t count,
                            int64_t* out_i64, uint8_t* out_ovf, uint32_t* out_mag, uint8_t* out_neg,
                            uint32_t* scratch, uint32_t* err, int grid, cudaStream_t st);
+// OU decryption over S-limb ciphertexts with Sp-limb p^2 arithmetic
+// (S, Sp) in {(64, 32), (128, 64), (128, 96)}.
+cudaError_t launch_ou_decrypt(int S, const KeyConst& kc, const OuConst& oc, const uint32_t* ct, size_t count,
+                              int64_t* out_i64, uint8_t* out_ovf, uint32_t* out_mag, uint8_t* out_neg,
+                              uint32_t* scratch, uint32_t* err, int grid, cudaStream_t st);
+cudaError_t ou_decrypt_geometry(int S, int Sp, int* grid, int* units_per_block);
+// Signed plaintexts -> non-negative exponents for the G and G^-1 tables.
+cudaError_t launch_ou_split_i64(const int64_t* p, int negate, uint32_t* ep, uint32_t* en, size_t count,
+                                cudaStream_t st);
+cudaError_t launch_ou_split_mag(const uint32_t* mag, const uint8_t* neg, int limbs, const uint32_t* maxpt,
+                                uint32_t* ep, uint32_t* en, size_t count, uint32_t* err, cudaStream_t st);
 cudaError_t launch_convert(int S, const KeyConst& kc, const uint32_t* in, uint32_t* out, size_t count,
                            int to_mont, uint32_t* err, cudaStream_t st);
 cudaError_t launch_reduce(int S, const KeyConst& kc, const uint32_t* in, size_t count, int chunk,

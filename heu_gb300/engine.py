@@ -63,6 +63,30 @@ def keygen(key_bits, seed):
     }
 
 
+def ou_sizes(key_bits):
+    """(ciphertext limbs S, secret limbs S/2) of an OU key."""
+    if key_bits == 1024:
+        return 64, 32
+    if key_bits in (2048, 3072):
+        return 128, 64
+    raise ValueError("OU keys of 1024, 2048 or 3072 bits")
+
+
+def ou_keygen(key_bits, seed):
+    """ou/key_generator.cc:26-96 from a seeded stream -> dict of ints n, G, H,
+    p, q, t, gp_inv and max_pt_bits."""
+    lib = capi.load()
+    S, H = ou_sizes(key_bits)
+    bufs = {k: np.zeros(S if k in ("n", "G", "H") else H, np.uint32) for k in ("n", "G", "H", "p", "q", "t", "gp_inv")}
+    mb = ctypes.c_int()
+    capi.check(lib.hg_ou_keygen(key_bits, seed & (2 ** 64 - 1), *[_ptr(bufs[k]) for k in ("n", "G", "H", "p", "q", "t",
+                                                                                        "gp_inv")],
+                                ctypes.byref(mb)))
+    out = {k: limbs_to_ints(v)[0] for k, v in bufs.items()}
+    out["max_pt_bits"] = mb.value
+    return out
+
+
 class Context:
     """One engine context on one device (hg_ctx)."""
 
@@ -86,6 +110,16 @@ class Context:
 
     def sm_count(self):
         return self.lib.hg_device_sm_count(self.handle)
+
+    def load_ou_key(self, key_bits, n, G, H, max_pt_bits, p=None, q=None, t=None, gp_inv=None, table_window=0):
+        """An Okamoto-Uchiyama key (ou/public_key.cc, secret_key.h) -> Key."""
+        S, Hh = ou_sizes(key_bits)
+        L = lambda v, k: ints_to_limbs([v], k) if v is not None else None  # noqa: E731
+        kid = ctypes.c_int()
+        capi.check(self.lib.hg_ou_key_load(self.handle, key_bits, _ptr(L(n, S)), _ptr(L(G, S)), _ptr(L(H, S)),
+                                           max_pt_bits, _ptr(L(p, Hh)), _ptr(L(q, Hh)), _ptr(L(t, Hh)),
+                                           _ptr(L(gp_inv, Hh)), table_window, ctypes.byref(kid)))
+        return Key(self, kid.value, key_bits, n)
 
     def load_key(self, key_bits, n, h_s, p=None, q=None, table_window=0):
         S = key_bits // 16

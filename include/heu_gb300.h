@@ -77,6 +77,29 @@ int hg_keygen(uint32_t key_bits, uint64_t seed, uint32_t* n_out, uint32_t* p_out
 int hg_key_load(hg_ctx* ctx, uint32_t key_bits, const uint32_t* n, const uint32_t* h_s, const uint32_t* p,
                 const uint32_t* q, int table_window, int* key_id);
 int hg_key_free(hg_ctx* ctx, int key_id);
+
+/* ---- Okamoto-Uchiyama keys ------------------------------------------------
+ * No counterpart in HEU's GPU code: the engine also serves HEU's OU scheme
+ * (heu/library/algorithms/ou).  hg_ou_keygen follows ou/key_generator.cc:
+ * 26-96 with every random draw from a seeded xoshiro256** stream.  n = p^2 q,
+ * G, H: S limbs (S = 64 for 1024-bit keys, 128 for 2048 / 3072); p, q, t
+ * (the large prime factor of p - 1), gp_inv: S/2 limbs; max_pt_bits:
+ * log2 of the plaintext bound (ou/key_generator.cc:86).
+ * hg_ou_key_load uploads the fixed-base tables of H (randomness, < 2^128), G
+ * and G^-1 (plaintexts) and, if the secret part is given, the decryption
+ * constants.  The returned key id works with hg_encrypt / encrypt_bn /
+ * encrypt_zero / randomize / decrypt / decrypt_bn / add / add_plain / sub /
+ * sub_plain / plain_sub / mul / negate / sum / bucket_sum / matmul / to_mont /
+ * from_mont and their hg_dev_ forms, with OU semantics (ou/encryptor.cc,
+ * decryptor.cc, evaluator.cc): c = H^r G^m mod n in Montgomery form with
+ * R = 2^(32 S); r < 2^80 / 2^110 / 2^128 by key size (4 limbs per r);
+ * plaintexts |m| <= 2^max_pt_bits.  Batches, the server and the autotuner
+ * serve ZPaillier keys only (HG_ERR_UNSUPPORTED otherwise).                */
+int hg_ou_keygen(uint32_t key_bits, uint64_t seed, uint32_t* n_out, uint32_t* G_out, uint32_t* H_out,
+                 uint32_t* p_out, uint32_t* q_out, uint32_t* t_out, uint32_t* gpinv_out, int* max_pt_bits);
+int hg_ou_key_load(hg_ctx* ctx, uint32_t key_bits, const uint32_t* n, const uint32_t* G, const uint32_t* H,
+                   int max_pt_bits, const uint32_t* p, const uint32_t* q, const uint32_t* t, const uint32_t* gp_inv,
+                   int table_window, int* key_id);
 /* limbs of one ciphertext (S) and of one r value for a loaded key */
 int hg_key_shape(hg_ctx* ctx, int key_id, int* ct_limbs, int* r_limbs, int* pt_limbs);
 
