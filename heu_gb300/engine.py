@@ -114,11 +114,13 @@ class Context:
     def load_ou_key(self, key_bits, n, G, H, max_pt_bits, p=None, q=None, t=None, gp_inv=None, table_window=0):
         """An Okamoto-Uchiyama key (ou/public_key.cc, secret_key.h) -> Key."""
         S, Hh = ou_sizes(key_bits)
-        L = lambda v, k: ints_to_limbs([v], k) if v is not None else None  # noqa: E731
+        # keep every limb array alive until the call returns
+        arrs = [ints_to_limbs([v], k) if v is not None else None
+                for v, k in ((n, S), (G, S), (H, S), (p, Hh), (q, Hh), (t, Hh), (gp_inv, Hh))]
         kid = ctypes.c_int()
-        capi.check(self.lib.hg_ou_key_load(self.handle, key_bits, _ptr(L(n, S)), _ptr(L(G, S)), _ptr(L(H, S)),
-                                           max_pt_bits, _ptr(L(p, Hh)), _ptr(L(q, Hh)), _ptr(L(t, Hh)),
-                                           _ptr(L(gp_inv, Hh)), table_window, ctypes.byref(kid)))
+        capi.check(self.lib.hg_ou_key_load(self.handle, key_bits, _ptr(arrs[0]), _ptr(arrs[1]), _ptr(arrs[2]),
+                                           max_pt_bits, _ptr(arrs[3]), _ptr(arrs[4]), _ptr(arrs[5]), _ptr(arrs[6]),
+                                           table_window, ctypes.byref(kid)))
         return Key(self, kid.value, key_bits, n)
 
     def load_key(self, key_bits, n, h_s, p=None, q=None, table_window=0):
