@@ -756,6 +756,131 @@ def c3_arm(args):
     return 0
 
 
+def ou_arm(args):
+    """Okamoto-Uchiyama (HEU's ou scheme) on one GB300: 2048-bit key from
+    seed 0, 2^20 int64 plaintexts in [-2^40, 2^40), r < 2^110; one step =
+    Encrypt + Add + Mul (64-bit k) + Decrypt over the batch, with the OU
+    oracle timed on a bounded sample on one host core."""
+    import numpy as np
+    import torch
+
+    import heu_gb300 as hg
+    import heu_gb300.engine as eng
+    from heu_gb300 import capi
+
+    dev = torch.device("cuda", 0)
+    kp = eng.ou_keygen(2048, 0)
+    ctx = hg.Context(0)
+    key = ctx.load_ou_key(2048, kp["n"], kp["G"], kp["H"], kp["max_pt_bits"], kp["p"], kp["q"], kp["t"],
+                          kp["gp_inv"], table_window=16)
+    lib, h = ctx.lib, ctx.handle
+    n, S = args.n, key.ct_limbs
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(21)
+    m = torch.randint(-(2 ** M_BITS), 2 ** M_BITS, (n,), dtype=torch.int64, device=dev, generator=gen)
+    r = torch.randint(-(2 ** 31), 2 ** 31, (n, key.r_limbs), dtype=torch.int32, device=dev, generator=gen)
+    r[:, 3] &= (1 << (110 - 96)) - 1
+    kk = torch.randint(-(2 ** 63), 2 ** 63 - 1, (n,), dtype=torch.int64, device=dev, generator=gen)
+    ct = torch.empty((n, S), dtype=torch.int32, device=dev)
+    cs = torch.empty_like(ct)
+    cm = torch.empty_like(ct)
+    d = torch.empty((n,), dtype=torch.int64, device=dev)
+    ovf = torch.empty((n,), dtype=torch.uint8, device=dev)
+    st = torch.cuda.Stream(device=dev)
+    sp = ctypes.c_void_p(st.cuda_stream)
+
+    def P(t):
+        return ctypes.c_void_p(t.data_ptr())
+
+    names = ("encrypt", "add", "mul", "decrypt")
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(5)] for _ in range(max(args.steps, 1))]
+
+    def step(e=None):
+        with torch.cuda.stream(st):
+            e and e[0].record(st)
+            capi.check(lib.hg_dev_encrypt(h, key.id, P(m), P(r), P(ct), n, sp))
+            e and e[1].record(st)
+            capi.check(lib.hg_dev_add(h, key.id, P(ct), P(ct), P(cs), n, sp))
+            e and e[2].record(st)
+            capi.check(lib.hg_dev_mul(h, key.id, P(ct), P(kk), P(cm), n, sp))
+            e and e[3].record(st)
+            capi.check(lib.hg_dev_decrypt(h, key.id, P(cs), P(d), P(ovf), n, sp))
+            e and e[4].record(st)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    capi.check(lib.hg_dev_check(h))
+    clk = ClockSampler(0)
+    clk.start()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record(st)
+    for i in range(args.steps):
+        step(ev[i])
+    t1.record(st)
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    capi.check(lib.hg_dev_check(h))
+    assert int(ovf.sum().item()) == 0 and torch.equal(d, 2 * m), "OU decrypt mismatch"
+    elapsed = t0.elapsed_time(t1) / 1e3
+    op_s = {nm: sum(ev[i][j].elapsed_time(ev[i][j + 1]) for i in range(args.steps)) / 1e3 / args.steps
+            for j, nm in enumerate(names)}
+    w, wd = 16, 5
+    t_bits = kp["t"].bit_length()
+    work = {
+        "encrypt": (-(-64 // w) + -(-110 // w)) * mm_macs(S) * n,
+        "add": mm_macs(S) * n,
+        "mul": mul_macs(2048, kk[: 1 << 14].cpu().numpy()) * (n / min(n, 1 << 14)),
+        "decrypt": ((t_bits - 1) + -(-t_bits // (wd + 1)) + 2 ** (wd - 1) + 3) * mm_macs(64) * n,
+    }
+    peak = max(capi.mac_peak(0, 0), capi.mac_peak(0, 1)) / 1e12
+    tmacs = {nm: work[nm] / op_s[nm] / 1e12 for nm in names}
+    # the OU oracle on one host core, bounded sample
+    from oracle import ou
+    from oracle.prg import Prg
+
+    pk = ou.PublicKey(kp["n"], kp["G"], kp["H"], 1 << kp["max_pt_bits"])
+    sk = ou.SecretKey(kp["p"], kp["q"], kp["t"], kp["gp_inv"])
+    prg = Prg(5)
+    ns = 400
+    ms = [prg.int64_uniform(-(2 ** M_BITS), 2 ** M_BITS) for _ in range(ns)]
+    rs = [prg.randbits(110) for _ in range(ns)]
+    ks = [prg.int64_uniform(-(2 ** 63), 2 ** 63) for _ in range(ns)]
+    rates = {}
+    t = time.perf_counter()
+    zs = [ou.encrypt(pk, a, b) for a, b in zip(ms, rs)]
+    rates["encrypt"] = ns / (time.perf_counter() - t)
+    t = time.perf_counter()
+    ss = [ou.add(pk, z, z) for z in zs]
+    rates["add"] = ns / (time.perf_counter() - t)
+    t = time.perf_counter()
+    [ou.mul(pk, z, k) for z, k in zip(zs[:100], ks[:100])]
+    rates["mul"] = 100 / (time.perf_counter() - t)
+    t = time.perf_counter()
+    dd = [ou.decrypt(pk, sk, z) for z in ss[:200]]
+    rates["decrypt"] = 200 / (time.perf_counter() - t)
+    assert dd == [2 * a for a in ms[:200]]
+    cpu_rate = 4.0 / sum(1.0 / rates[o] for o in names)
+    line = {
+        "metric": "OU-2048 ops/s (enc/add/mul/dec)", "value": 4 * n * args.steps / elapsed, "unit": UNIT,
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": "ou: 2048-bit OU key (n of %d bits), 2^20 int64 m~U[-2^40,2^40), r<2^110, "
+                               "enc+add+mul(64-bit k)+dec per step" % kp["n"].bit_length(),
+                   "table_window": w, "ciphertext_limbs": S},
+        "per_op_ops_per_s": {nm: n / op_s[nm] for nm in names},
+        "roofline": {"bound": "imad", "unit": "TMAC/s", "per_op_tmacs": tmacs, "peak": peak,
+                     "frac": {nm: tmacs[nm] / peak for nm in names}},
+        "cpu_baseline": {"value": cpu_rate, "unit": UNIT, "cores": 1, "kind": "port", "per_op": rates,
+                         "sample": f"OU oracle (Python integers), {ns} enc/add, 100 mul, 200 dec, one core"},
+        "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+    ctx.close()
+    return 0
+
+
 def c5_arm(args):
     """Config 5: served request stream.  8 resident keypairs (six 2048-bit,
     two 3072-bit), Poisson arrivals at swept rates, lengths log-uniform in
@@ -918,7 +1043,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", choices=["config2", "config3", "config4", "config5"], default="config2")
+    ap.add_argument("--workload", choices=["config2", "config3", "config4", "config5", "ou"], default="config2")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner")
     ap.add_argument("--key-config", default=None,
                     help="explicit key config instead of the autotuner, e.g. "
@@ -943,6 +1068,8 @@ def main():
         return c3_arm(args)
     if args.workload == "config5":
         return c5_arm(args)
+    if args.workload == "ou":
+        return ou_arm(args)
     return ours_arm(args)
 
 
