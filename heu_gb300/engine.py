@@ -72,6 +72,16 @@ def ou_sizes(key_bits):
     raise ValueError("OU keys of 1024, 2048 or 3072 bits")
 
 
+def ou_random_bits(n_bits):
+    """Bit length of OU encryption randomness for an n of n_bits bits
+    (ou/encryptor.cc:12-20 with ou/public_key.h:27-31): 80 / 110 / 128."""
+    if n_bits >= 2560:
+        return 128
+    if n_bits >= 1536:
+        return 110
+    return 80
+
+
 def ou_keygen(key_bits, seed):
     """ou/key_generator.cc:26-96 from a seeded stream -> dict of ints n, G, H,
     p, q, t, gp_inv and max_pt_bits."""

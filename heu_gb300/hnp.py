@@ -7,10 +7,12 @@ and ``array()``; the evaluator offers add / sub / mul (with NumPy broadcasting
 of the two shapes, numpy/evaluator.cc:160-185), matmul, sum, select_sum,
 batch_select_sum, feature_wise_bucket_sum and batch_feature_wise_bucket_sum.
 
-Plaintexts are integers (int64 NumPy arrays, or Python ints up to n/2 in an
-object array); HEU's encoders are not part of this path.  Ciphertexts are
-kept as a (size, S) uint32 limb array in Montgomery form with a logical
-shape, exactly the bytes the C-ABI exchanges.
+Two schemes: ZPaillier (the default) and OU (``setup(..., schema="ou")``,
+heu/library/algorithms/ou), both on the same kernels.  Plaintexts are
+integers (int64 NumPy arrays, or Python ints up to the scheme's plaintext
+bound in an object array); ``BatchEncoder`` packs two int64 values per
+plaintext.  Ciphertexts are kept as a (size, S) uint32 limb array in
+Montgomery form with a logical shape, exactly the bytes the C-ABI exchanges.
 """
 
 import os
@@ -150,24 +152,52 @@ class BatchEncoder:
 
 
 
-def setup(key_size=2048, seed=None, device=0, table_window=0, context=None):
-    """Key generation (key_generator.cc:26-60, seeded xoshiro256** stream; a
-    random seed when none is given) and engine key load -> HeKit."""
+SCHEMAS = ("zpaillier", "ou")
+
+
+def setup(key_size=2048, seed=None, device=0, table_window=0, context=None, schema="zpaillier"):
+    """Key generation (paillier_z/key_generator.cc:26-60 or
+    ou/key_generator.cc:26-96, seeded xoshiro256** stream; a random seed when
+    none is given) and engine key load -> HeKit.  ``schema`` names the scheme
+    the way heu.phe.setup's SchemaType does (ZPaillier or OU)."""
+    schema = schema.lower()
+    if schema not in SCHEMAS:
+        raise ValueError(f"schema must be one of {SCHEMAS}")
     if seed is None:
         seed = int.from_bytes(os.urandom(8), "little")
-    k = engine.keygen(key_size, seed)
     ctx = context or engine.Context(device)
-    key = ctx.load_key(key_size, k["n"], k["h_s"], k["p"], k["q"], table_window=table_window)
-    return HeKit(ctx, key, k)
+    if schema == "ou":
+        k = engine.ou_keygen(key_size, seed)
+        key = ctx.load_ou_key(key_size, k["n"], k["G"], k["H"], k["max_pt_bits"], k["p"], k["q"], k["t"],
+                              k["gp_inv"], table_window=table_window)
+    else:
+        k = engine.keygen(key_size, seed)
+        key = ctx.load_key(key_size, k["n"], k["h_s"], k["p"], k["q"], table_window=table_window)
+    return HeKit(ctx, key, k, schema)
 
 
 class HeKit:
-    def __init__(self, ctx, key, key_ints):
+    """Key material and engine key of one scheme.  ``max_plaintext`` is the
+    bound on |m| that Encrypt checks: n/2 for ZPaillier
+    (paillier_z/public_key.h PlaintextBound), 2^(|p/2|-1) for OU
+    (ou/key_generator.cc:89-92).  ``random_bits`` is the exact bit length of
+    the encryption randomness r, or None where r is any value below 2^(32*r_limbs)."""
+
+    def __init__(self, ctx, key, key_ints, schema="zpaillier"):
         self.context = ctx
         self.key = key
-        self.public_key = {"n": key_ints["n"], "h_s": key_ints["h_s"]}
-        self.secret_key = {"p": key_ints["p"], "q": key_ints["q"]}
+        self.schema = schema
         self.n = key_ints["n"]
+        if schema == "ou":
+            self.public_key = {k: key_ints[k] for k in ("n", "G", "H")}
+            self.secret_key = {k: key_ints[k] for k in ("p", "q", "t", "gp_inv")}
+            self.max_plaintext = 1 << key_ints["max_pt_bits"]
+            self.random_bits = engine.ou_random_bits(self.n.bit_length())
+        else:
+            self.public_key = {"n": key_ints["n"], "h_s": key_ints["h_s"]}
+            self.secret_key = {"p": key_ints["p"], "q": key_ints["q"]}
+            self.max_plaintext = self.n // 2
+            self.random_bits = None
 
     def array(self, values):
         return PlaintextArray(values)
@@ -199,6 +229,12 @@ class Encryptor:
         if self.r_source is not None:
             return np.ascontiguousarray(self.r_source(count), dtype=np.uint32).reshape(count, key.r_limbs)
         r = np.frombuffer(os.urandom(count * key.r_limbs * 4), dtype=np.uint32).reshape(count, key.r_limbs).copy()
+        bits = self.kit.random_bits
+        if bits is not None:  # RandomExactBits(bits): top bit set, nothing above it
+            top, off = divmod(bits - 1, 32)
+            r[:, top] &= np.uint32((1 << off) - 1)
+            r[:, top] |= np.uint32(1 << off)
+            r[:, top + 1:] = 0
         return r
 
     def encrypt(self, pt):
@@ -206,8 +242,8 @@ class Encryptor:
         key = self.kit.key
         flat = pt.values.reshape(-1)
         if flat.dtype == object:
-            half = self.kit.n // 2
-            if any(abs(int(v)) > half for v in flat):
+            bound = self.kit.max_plaintext
+            if any(abs(int(v)) > bound for v in flat):
                 raise ValueError("message number out of range")
             limbs = key.encrypt_bn([int(v) for v in flat], self._r(flat.size))
         else:

@@ -150,3 +150,37 @@ def test_batch_encoder_packed_ciphertexts(kit):
     assert int(f) == int(a1.sum()) and int(s) == int(b1.sum())
     f, s = dec.decrypt_batch(ev.mul(c1, kit.array(np.full(300, 3))), be)
     assert np.array_equal(f, a1 * 3) and np.array_equal(s, b1 * 3)
+
+
+@pytest.mark.parametrize("bits,seed", [(1024, 5), (2048, 0)])
+def test_ou_schema_through_the_numpy_layer(gpu_ctx, bits, seed):
+    """hnp.setup(schema="ou"): ciphertexts byte-equal to the OU oracle under the
+    same r, and the element-wise / reduction surface equal to integer math."""
+    from oracle import ou
+
+    kit = hnp.setup(bits, seed=seed, context=gpu_ctx, table_window=8, schema="ou")
+    pk = ou.PublicKey(kit.public_key["n"], kit.public_key["G"], kit.public_key["H"], kit.max_plaintext)
+    sk = ou.SecretKey(*(kit.secret_key[k] for k in ("p", "q", "t", "gp_inv")))
+    rng = np.random.default_rng(seed)
+    a = rng.integers(-10 ** 6, 10 ** 6, size=(3, 4))
+    b = rng.integers(-10 ** 6, 10 ** 6, size=(4,))
+    rs = [int(v) | (1 << (kit.random_bits - 1)) for v in rng.integers(1, 2 ** 62, size=12)]
+    enc = kit.encryptor(lambda count: hg.ints_to_limbs(rs[:count], kit.key.r_limbs))
+    dec, ev = kit.decryptor(), kit.evaluator()
+    x = enc.encrypt(kit.array(a))
+    want = [ou.to_mont(pk, ou.encrypt(pk, int(m), r)) for m, r in zip(a.reshape(-1), rs)]
+    assert hg.limbs_to_ints(x.limbs) == want
+    assert [ou.decrypt(pk, sk, ou.from_mont(pk, c)) for c in want] == a.reshape(-1).tolist()
+    enc = kit.encryptor()
+    y = enc.encrypt(kit.array(b))
+    assert np.array_equal(dec.decrypt(ev.add(x, y)).to_numpy(), a + b)
+    assert np.array_equal(dec.decrypt(ev.sub(x, kit.array(b))).to_numpy(), a - b)
+    assert np.array_equal(dec.decrypt(ev.mul(x, kit.array([3, -2, 0, 1]))).to_numpy(), a * [3, -2, 0, 1])
+    assert np.array_equal(dec.decrypt(ev.negate(ev.randomize(x))).to_numpy(), -a)
+    assert dec.decrypt(ev.sum(x)).to_numpy() == a.sum()
+    assert np.array_equal(dec.decrypt(ev.matmul(x, kit.array(np.eye(4, 2, dtype=np.int64)))).to_numpy(),
+                          a @ np.eye(4, 2, dtype=np.int64))
+    big = kit.max_plaintext
+    assert dec.decrypt(enc.encrypt(kit.array([big, -big]))).to_numpy().tolist() == [big, -big]
+    with pytest.raises(ValueError, match="out of range"):
+        enc.encrypt(kit.array([big + 1]))

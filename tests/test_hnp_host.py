@@ -50,3 +50,28 @@ def test_batch_encoder_packs_like_the_reference():
     assert e10.unpack(m10, 0).tolist() == [3, -4] and e10.unpack(m10, 1).tolist() == [-7, 8]
     with pytest.raises(ValueError):
         e.unpack(m, 2)
+
+
+def test_setup_rejects_unknown_schema():
+    with pytest.raises(ValueError, match="schema"):
+        hnp.setup(1024, seed=1, schema="elgamal")
+
+
+def test_ou_randomness_has_exact_bits():
+    """OU r is RandomExactBits(random_bits) (ou/encryptor.cc:12-33): the top
+    bit set and nothing above it, for 80 / 110 / 128-bit draws."""
+
+    class _Key:
+        r_limbs = 4
+
+    class _Kit:
+        key = _Key()
+
+    for n_bits, bits in ((1030, 80), (2051, 110), (3077, 128)):
+        from heu_gb300 import engine
+        assert engine.ou_random_bits(n_bits) == bits
+        kit = _Kit()
+        kit.random_bits = bits
+        r = hnp.Encryptor(kit)._r(64)
+        vals = [sum(int(w) << (32 * i) for i, w in enumerate(row)) for row in r]
+        assert all(v.bit_length() == bits for v in vals)
