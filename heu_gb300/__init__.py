@@ -1,4 +1,5 @@
-"""GB300-native Paillier engine with HEU ZPaillier (paillier_z) semantics.
+"""GB300-native Paillier engine with HEU ZPaillier (paillier_z) semantics,
+and HEU's Okamoto-Uchiyama (ou) scheme on the same kernels.
 
 The compute path is the CUDA library built from ``heu_gb300/csrc`` and
 reached through the C-ABI declared in ``include/heu_gb300.h``; there is no
@@ -6,6 +7,6 @@ CPU fallback.
 """
 
 from heu_gb300.capi import HgError, load  # noqa: F401
-from heu_gb300.engine import Context, Key, ints_to_limbs, keygen, limbs_to_ints  # noqa: F401
+from heu_gb300.engine import Context, Key, ints_to_limbs, keygen, limbs_to_ints, ou_keygen  # noqa: F401
 from heu_gb300.batch import Batch  # noqa: F401,E402
 from heu_gb300.server import Server  # noqa: F401,E402
