@@ -182,6 +182,8 @@ struct InvTask {
   volatile int status = 0;   // 0 ok, 1 not invertible, 2 range error upstream
 };
 
+// The status is sticky: a failure stays recorded until the caller resets it,
+// so one task can serve several inversions enqueued in one stream.
 void CUDART_CB inv_host_fn(void* p) {
   InvTask* t = static_cast<InvTask*>(p);
   const size_t S = (size_t)t->S;
@@ -191,10 +193,8 @@ void CUDART_CB inv_host_fn(void* p) {
     return;
   }
   // root = X*R; the tree's down-sweep wants X^-1 * R
-  if (hg::mont_root_inverse(t->root, *t->N, S, t->z)) {
-    t->status = 0;
-  } else {
-    t->status = 1;
+  if (!hg::mont_root_inverse(t->root, *t->N, S, t->z)) {
+    if (t->status == 0) t->status = 1;
     for (size_t i = 0; i < S; ++i) t->z[i] = 0u;
   }
 }
@@ -316,6 +316,79 @@ void h2d(void* d, const void* h, size_t bytes, Work& w) {
 }
 void d2h(void* h, const void* d, size_t bytes, Work& w) {
   if (bytes) cuda_check(cudaMemcpyAsync(h, d, bytes, cudaMemcpyDeviceToHost, w.stream), "D2H");
+}
+
+// Both lanes' error words, OR-ed: the same error a single lane would raise.
+void finish_pair(Work& a, Work& b) {
+  uint32_t* ha = a.pin_err.ensure<uint32_t>(sizeof(uint32_t));
+  uint32_t* hb = b.pin_err.ensure<uint32_t>(sizeof(uint32_t));
+  cuda_check(cudaMemcpyAsync(ha, a.errp(), sizeof(uint32_t), cudaMemcpyDeviceToHost, a.stream), "D2H err");
+  cuda_check(cudaMemcpyAsync(hb, b.errp(), sizeof(uint32_t), cudaMemcpyDeviceToHost, b.stream), "D2H err");
+  cuda_check(cudaStreamSynchronize(a.stream), "stream sync");
+  cuda_check(cudaStreamSynchronize(b.stream), "stream sync");
+  raise_err_bits(*ha | *hb);
+}
+
+// A second lane for one call, when one is free (never waits for one).
+struct ExtraLane {
+  hg_ctx* ctx;
+  Work* w = nullptr;
+  explicit ExtraLane(hg_ctx* c) : ctx(c) {
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    if (!ctx->free_lanes.empty()) {
+      w = ctx->free_lanes.back();
+      ctx->free_lanes.pop_back();
+    }
+  }
+  ~ExtraLane() {
+    if (!w) return;
+    {
+      std::lock_guard<std::mutex> lk(ctx->mu);
+      ctx->free_lanes.push_back(w);
+    }
+    ctx->lane_cv.notify_one();
+  }
+};
+
+// Host-pointer calls over many elements run as up to kPipeMaxChunks chunks
+// alternating between the caller's lane and a second free lane: each chunk is
+// H2D -> kernels -> D2H in its own lane's stream order, so one lane's copies
+// run while the other lane's kernels compute.  chunk(w, offset, count)
+// enqueues one chunk; the call returns after both lanes drained.
+constexpr size_t kPipeMinChunk = (size_t)1 << 16;
+constexpr size_t kPipeMaxChunks = 8;
+
+// prepare(w) runs on each lane before its first chunk, check(w) on each lane
+// after both drained (the error words are raised first).
+template <class F, class Prep, class Check>
+void run_chunked(hg_ctx* ctx, Work& w0, size_t count, F&& chunk, Prep&& prepare, Check&& check) {
+  if (count >= 2 * kPipeMinChunk) {
+    ExtraLane extra(ctx);
+    if (extra.w) {
+      Work& w1 = *extra.w;
+      reset_err(w1);
+      prepare(w0);
+      prepare(w1);
+      const size_t nch = std::min(kPipeMaxChunks, count / kPipeMinChunk);
+      const size_t per = (count + nch - 1) / nch;
+      Work* lanes[2] = {&w0, &w1};
+      size_t c = 0;
+      for (size_t off = 0; off < count; off += per, ++c) chunk(*lanes[c & 1], off, std::min(per, count - off));
+      finish_pair(w0, w1);
+      check(w0);
+      check(w1);
+      return;
+    }
+  }
+  prepare(w0);
+  chunk(w0, (size_t)0, count);
+  finish(w0);
+  check(w0);
+}
+
+template <class F>
+void run_chunked(hg_ctx* ctx, Work& w0, size_t count, F&& chunk) {
+  run_chunked(ctx, w0, count, std::forward<F>(chunk), [](Work&) {}, [](Work&) {});
 }
 
 // ---------------------------------------------------------------------------
@@ -445,19 +518,29 @@ void raise_task_status(const InvTask& t) {
   if (t.status == 1) fail(HG_ERR_NOT_INVERTIBLE, "ciphertext not invertible mod n^2 (Negate/Sub/Mul with k<0)");
 }
 
-// Synchronous form used by the host-pointer and device-pointer calls.
-void core_inverse(KeyRec& k, Work& w, const uint32_t* in, const int64_t* sel, uint32_t* out, size_t count) {
+// The lane's inversion in stream order; w.task.status (reset by the caller)
+// records a failure once the stream has run it.
+void core_inverse_enqueue(KeyRec& k, Work& w, const uint32_t* in, const int64_t* sel, uint32_t* out,
+                          size_t count) {
   if (count == 0) return;
   w.task.root = w.pin_root.ensure<uint32_t>((size_t)k.S * 4 + 4);
   w.task.z = w.pin_z.ensure<uint32_t>((size_t)k.S * 4);
-  w.task.status = 0;
   core_inverse_async(k, in, sel, out, count, w.inv, w.task, w.errp(), w.stream);
+}
+
+// Synchronous form used by the host-pointer and device-pointer calls.
+void core_inverse(KeyRec& k, Work& w, const uint32_t* in, const int64_t* sel, uint32_t* out, size_t count) {
+  if (count == 0) return;
+  w.task.status = 0;
+  core_inverse_enqueue(k, w, in, sel, out, count);
   cuda_check(cudaStreamSynchronize(w.stream), "stream sync");
   raise_task_status(w.task);
 }
 
+// sync_inverse = false leaves the inversion (k < 0) in stream order: the
+// caller resets w.task.status first and checks it after the stream drained.
 void core_mul(KeyRec& k, Work& w, const uint32_t* a, const int64_t* kk, const int64_t* host_k, uint32_t* out,
-              size_t count) {
+              size_t count, bool sync_inverse = true) {
   const size_t ntab = (size_t)1 << (k.wm - 1);
   const size_t inst = (size_t)k.grid_mul * hg::instances_per_block(k.S, k.kc.variant);
   uint32_t* scratch = w.scratch.ensure<uint32_t>(inst * ntab * k.S * 4);
@@ -468,7 +551,12 @@ void core_mul(KeyRec& k, Work& w, const uint32_t* a, const int64_t* kk, const in
     any_neg = false;
     for (size_t i = 0; i < count && !any_neg; ++i) any_neg = host_k[i] < 0;
   }
-  if (any_neg) core_inverse(k, w, out, kk, out, count);
+  if (any_neg) {
+    if (sync_inverse)
+      core_inverse(k, w, out, kk, out, count);
+    else
+      core_inverse_enqueue(k, w, out, kk, out, count);
+  }
 }
 
 void core_sum(KeyRec& k, Work& w, const uint32_t* a, size_t count, uint32_t* out) {
@@ -1127,14 +1215,15 @@ int hg_encrypt(hg_ctx* ctx, int key_id, const int64_t* m, const uint32_t* r, uin
     if (!m || !r || !ct_out) fail(HG_ERR_INVALID, "null argument");
     HG_HOST_PROLOGUE
     const size_t rb = (size_t)k->kc.rlimbs * 4;
-    auto* dm = w.io[0].ensure<int64_t>(count * 8);
-    auto* dr = w.io[1].ensure<uint32_t>(count * rb);
-    auto* dout = w.io[2].ensure<uint32_t>(count * cb);
-    h2d(dm, m, count * 8, w);
-    h2d(dr, r, count * rb, w);
-    core_encrypt(*k, w, hg::EncMode::kEncrypt, dm, nullptr, nullptr, dr, nullptr, dout, count);
-    d2h(ct_out, dout, count * cb, w);
-    finish(w);
+    run_chunked(ctx, w, count, [&](Work& v, size_t off, size_t cnt) {
+      auto* dm = v.io[0].ensure<int64_t>(cnt * 8);
+      auto* dr = v.io[1].ensure<uint32_t>(cnt * rb);
+      auto* dout = v.io[2].ensure<uint32_t>(cnt * cb);
+      h2d(dm, m + off, cnt * 8, v);
+      h2d(dr, (const uint8_t*)r + off * rb, cnt * rb, v);
+      core_encrypt(*k, v, hg::EncMode::kEncrypt, dm, nullptr, nullptr, dr, nullptr, dout, cnt);
+      d2h((uint8_t*)ct_out + off * cb, dout, cnt * cb, v);
+    });
     return HG_OK;
   });
 }
@@ -1145,16 +1234,17 @@ int hg_encrypt_bn(hg_ctx* ctx, int key_id, const uint32_t* m_mag, const uint8_t*
     if (!m_mag || !m_neg || !r || !ct_out) fail(HG_ERR_INVALID, "null argument");
     HG_HOST_PROLOGUE
     const size_t rb = (size_t)k->kc.rlimbs * 4, pb = (size_t)(k->scheme == 1 ? k->pt_limbs : k->S / 2) * 4;
-    auto* dmag = w.io[0].ensure<uint32_t>(count * pb);
-    auto* dneg = w.io[3].ensure<uint8_t>(count);
-    auto* dr = w.io[1].ensure<uint32_t>(count * rb);
-    auto* dout = w.io[2].ensure<uint32_t>(count * cb);
-    h2d(dmag, m_mag, count * pb, w);
-    h2d(dneg, m_neg, count, w);
-    h2d(dr, r, count * rb, w);
-    core_encrypt(*k, w, hg::EncMode::kEncrypt, nullptr, dmag, dneg, dr, nullptr, dout, count);
-    d2h(ct_out, dout, count * cb, w);
-    finish(w);
+    run_chunked(ctx, w, count, [&](Work& v, size_t off, size_t cnt) {
+      auto* dmag = v.io[0].ensure<uint32_t>(cnt * pb);
+      auto* dneg = v.io[3].ensure<uint8_t>(cnt);
+      auto* dr = v.io[1].ensure<uint32_t>(cnt * rb);
+      auto* dout = v.io[2].ensure<uint32_t>(cnt * cb);
+      h2d(dmag, (const uint8_t*)m_mag + off * pb, cnt * pb, v);
+      h2d(dneg, m_neg + off, cnt, v);
+      h2d(dr, (const uint8_t*)r + off * rb, cnt * rb, v);
+      core_encrypt(*k, v, hg::EncMode::kEncrypt, nullptr, dmag, dneg, dr, nullptr, dout, cnt);
+      d2h((uint8_t*)ct_out + off * cb, dout, cnt * cb, v);
+    });
     return HG_OK;
   });
 }
@@ -1164,12 +1254,13 @@ int hg_encrypt_zero(hg_ctx* ctx, int key_id, const uint32_t* r, uint32_t* ct_out
     if (!r || !ct_out) fail(HG_ERR_INVALID, "null argument");
     HG_HOST_PROLOGUE
     const size_t rb = (size_t)k->kc.rlimbs * 4;
-    auto* dr = w.io[1].ensure<uint32_t>(count * rb);
-    auto* dout = w.io[2].ensure<uint32_t>(count * cb);
-    h2d(dr, r, count * rb, w);
-    core_encrypt(*k, w, hg::EncMode::kZero, nullptr, nullptr, nullptr, dr, nullptr, dout, count);
-    d2h(ct_out, dout, count * cb, w);
-    finish(w);
+    run_chunked(ctx, w, count, [&](Work& v, size_t off, size_t cnt) {
+      auto* dr = v.io[1].ensure<uint32_t>(cnt * rb);
+      auto* dout = v.io[2].ensure<uint32_t>(cnt * cb);
+      h2d(dr, (const uint8_t*)r + off * rb, cnt * rb, v);
+      core_encrypt(*k, v, hg::EncMode::kZero, nullptr, nullptr, nullptr, dr, nullptr, dout, cnt);
+      d2h((uint8_t*)ct_out + off * cb, dout, cnt * cb, v);
+    });
     return HG_OK;
   });
 }
@@ -1179,13 +1270,14 @@ int hg_randomize(hg_ctx* ctx, int key_id, uint32_t* ct, const uint32_t* r, size_
     if (!r || !ct) fail(HG_ERR_INVALID, "null argument");
     HG_HOST_PROLOGUE
     const size_t rb = (size_t)k->kc.rlimbs * 4;
-    auto* dr = w.io[1].ensure<uint32_t>(count * rb);
-    auto* dc = w.io[2].ensure<uint32_t>(count * cb);
-    h2d(dr, r, count * rb, w);
-    h2d(dc, ct, count * cb, w);
-    core_encrypt(*k, w, hg::EncMode::kRandomize, nullptr, nullptr, nullptr, dr, dc, dc, count);
-    d2h(ct, dc, count * cb, w);
-    finish(w);
+    run_chunked(ctx, w, count, [&](Work& v, size_t off, size_t cnt) {
+      auto* dr = v.io[1].ensure<uint32_t>(cnt * rb);
+      auto* dc = v.io[2].ensure<uint32_t>(cnt * cb);
+      h2d(dr, (const uint8_t*)r + off * rb, cnt * rb, v);
+      h2d(dc, (const uint8_t*)ct + off * cb, cnt * cb, v);
+      core_encrypt(*k, v, hg::EncMode::kRandomize, nullptr, nullptr, nullptr, dr, dc, dc, cnt);
+      d2h((uint8_t*)ct + off * cb, dc, cnt * cb, v);
+    });
     return HG_OK;
   });
 }
@@ -1194,14 +1286,15 @@ int hg_decrypt(hg_ctx* ctx, int key_id, const uint32_t* ct, int64_t* m_out, uint
   return guarded(__func__, [&] {
     if (!ct || !m_out) fail(HG_ERR_INVALID, "null argument");
     HG_HOST_PROLOGUE
-    auto* dc = w.io[0].ensure<uint32_t>(count * cb);
-    auto* dm = w.io[1].ensure<int64_t>(count * 8);
-    auto* dov = w.io[2].ensure<uint8_t>(count);
-    h2d(dc, ct, count * cb, w);
-    core_decrypt(*k, w, dc, dm, dov, nullptr, nullptr, count);
-    d2h(m_out, dm, count * 8, w);
-    if (overflow) d2h(overflow, dov, count, w);
-    finish(w);
+    run_chunked(ctx, w, count, [&](Work& v, size_t off, size_t cnt) {
+      auto* dc = v.io[0].ensure<uint32_t>(cnt * cb);
+      auto* dm = v.io[1].ensure<int64_t>(cnt * 8);
+      auto* dov = v.io[2].ensure<uint8_t>(cnt);
+      h2d(dc, (const uint8_t*)ct + off * cb, cnt * cb, v);
+      core_decrypt(*k, v, dc, dm, dov, nullptr, nullptr, cnt);
+      d2h(m_out + off, dm, cnt * 8, v);
+      if (overflow) d2h(overflow + off, dov, cnt, v);
+    });
     return HG_OK;
   });
 }
@@ -1211,14 +1304,15 @@ int hg_decrypt_bn(hg_ctx* ctx, int key_id, const uint32_t* ct, uint32_t* m_mag, 
     if (!ct || !m_mag || !m_neg) fail(HG_ERR_INVALID, "null argument");
     HG_HOST_PROLOGUE
     const size_t pb = (size_t)(k->scheme == 1 ? k->pt_limbs : k->S / 2) * 4;
-    auto* dc = w.io[0].ensure<uint32_t>(count * cb);
-    auto* dmag = w.io[1].ensure<uint32_t>(count * pb);
-    auto* dneg = w.io[2].ensure<uint8_t>(count);
-    h2d(dc, ct, count * cb, w);
-    core_decrypt(*k, w, dc, nullptr, nullptr, dmag, dneg, count);
-    d2h(m_mag, dmag, count * pb, w);
-    d2h(m_neg, dneg, count, w);
-    finish(w);
+    run_chunked(ctx, w, count, [&](Work& v, size_t off, size_t cnt) {
+      auto* dc = v.io[0].ensure<uint32_t>(cnt * cb);
+      auto* dmag = v.io[1].ensure<uint32_t>(cnt * pb);
+      auto* dneg = v.io[2].ensure<uint8_t>(cnt);
+      h2d(dc, (const uint8_t*)ct + off * cb, cnt * cb, v);
+      core_decrypt(*k, v, dc, nullptr, nullptr, dmag, dneg, cnt);
+      d2h((uint8_t*)m_mag + off * pb, dmag, cnt * pb, v);
+      d2h(m_neg + off, dneg, cnt, v);
+    });
     return HG_OK;
   });
 }
@@ -1227,13 +1321,14 @@ int hg_add(hg_ctx* ctx, int key_id, const uint32_t* a, const uint32_t* b, uint32
   return guarded(__func__, [&] {
     if (!a || !b || !out) fail(HG_ERR_INVALID, "null argument");
     HG_HOST_PROLOGUE
-    auto* da = w.io[0].ensure<uint32_t>(count * cb);
-    auto* db = w.io[1].ensure<uint32_t>(count * cb);
-    h2d(da, a, count * cb, w);
-    h2d(db, b, count * cb, w);
-    cuda_check(hg::launch_add(k->S, k->kc, da, db, da, count, w.errp(), w.stream), "add launch");
-    d2h(out, da, count * cb, w);
-    finish(w);
+    run_chunked(ctx, w, count, [&](Work& v, size_t off, size_t cnt) {
+      auto* da = v.io[0].ensure<uint32_t>(cnt * cb);
+      auto* db = v.io[1].ensure<uint32_t>(cnt * cb);
+      h2d(da, (const uint8_t*)a + off * cb, cnt * cb, v);
+      h2d(db, (const uint8_t*)b + off * cb, cnt * cb, v);
+      cuda_check(hg::launch_add(k->S, k->kc, da, db, da, cnt, v.errp(), v.stream), "add launch");
+      d2h((uint8_t*)out + off * cb, da, cnt * cb, v);
+    });
     return HG_OK;
   });
 }
@@ -1243,13 +1338,14 @@ static int add_plain_impl(hg_ctx* ctx, int key_id, const uint32_t* a, const int6
   return guarded(__func__, [&] {
     if (!a || !p || !out) fail(HG_ERR_INVALID, "null argument");
     HG_HOST_PROLOGUE
-    auto* da = w.io[0].ensure<uint32_t>(count * cb);
-    auto* dp = w.io[1].ensure<int64_t>(count * 8);
-    h2d(da, a, count * cb, w);
-    h2d(dp, p, count * 8, w);
-    core_add_plain(*k, w, da, dp, neg, da, count);
-    d2h(out, da, count * cb, w);
-    finish(w);
+    run_chunked(ctx, w, count, [&](Work& v, size_t off, size_t cnt) {
+      auto* da = v.io[0].ensure<uint32_t>(cnt * cb);
+      auto* dp = v.io[1].ensure<int64_t>(cnt * 8);
+      h2d(da, (const uint8_t*)a + off * cb, cnt * cb, v);
+      h2d(dp, p + off, cnt * 8, v);
+      core_add_plain(*k, v, da, dp, neg, da, cnt);
+      d2h((uint8_t*)out + off * cb, da, cnt * cb, v);
+    });
     return HG_OK;
   });
 }
@@ -1313,14 +1409,15 @@ int hg_mul(hg_ctx* ctx, int key_id, const uint32_t* a, const int64_t* kk, uint32
   return guarded(__func__, [&] {
     if (!a || !kk || !out) fail(HG_ERR_INVALID, "null argument");
     HG_HOST_PROLOGUE
-    auto* da = w.io[0].ensure<uint32_t>(count * cb);
-    auto* dk = w.io[1].ensure<int64_t>(count * 8);
-    auto* dout = w.io[2].ensure<uint32_t>(count * cb);
-    h2d(da, a, count * cb, w);
-    h2d(dk, kk, count * 8, w);
-    core_mul(*k, w, da, dk, kk, dout, count);
-    d2h(out, dout, count * cb, w);
-    finish(w);
+    run_chunked(ctx, w, count, [&](Work& v, size_t off, size_t cnt) {
+      auto* da = v.io[0].ensure<uint32_t>(cnt * cb);
+      auto* dk = v.io[1].ensure<int64_t>(cnt * 8);
+      auto* dout = v.io[2].ensure<uint32_t>(cnt * cb);
+      h2d(da, (const uint8_t*)a + off * cb, cnt * cb, v);
+      h2d(dk, kk + off, cnt * 8, v);
+      core_mul(*k, v, da, dk, kk + off, dout, cnt, false);
+      d2h((uint8_t*)out + off * cb, dout, cnt * cb, v);
+    }, [](Work& v) { v.task.status = 0; }, [](Work& v) { raise_task_status(v.task); });
     return HG_OK;
   });
 }

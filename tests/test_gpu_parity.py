@@ -460,3 +460,79 @@ def test_host_api_is_thread_safe(gpu_key):
     for t in ths:
         t.join()
     assert not errors, errors
+
+
+def test_chunked_host_calls_match_single_lane_calls(gpu_key):
+    """Host-pointer calls of >= 2^17 elements run as chunks alternating over two
+    lanes; every element equals what an unchunked call gives, and an error in
+    a chunk on either lane (range, non-invertible) is raised as before."""
+    key, pk, sk = gpu_key(1024, 1)
+    n = 3 * (1 << 16) + 123  # three chunks: lanes A, B, A
+    per = -(-n // 3)
+    rng = np.random.default_rng(31)
+    m = rng.integers(-(2 ** 40), 2 ** 40, size=n, dtype=np.int64)
+    r = rng.integers(0, 2 ** 32, size=(n, key.r_limbs), dtype=np.uint64).astype(np.uint32)
+    k = rng.integers(-(2 ** 20), 2 ** 20, size=n, dtype=np.int64)
+    ct = key.encrypt(m, r)
+    d, ovf = key.decrypt(ct)
+    assert ovf.sum() == 0 and np.array_equal(d, m)
+    ct2 = key.encrypt(m[::-1].copy(), r)
+    s = key.add(ct, ct2)
+    ml = key.mul(ct, k)
+    ez = key.encrypt_zero(r)
+    rz = key.randomize(ct, r[::-1].copy())
+    ap = key.add_plain(ct, k)
+    for lo, hi in ((0, 5), (per - 4, per + 4), (2 * per - 3, 2 * per + 3), (n - 5, n)):
+        sl = slice(lo, hi)
+        assert np.array_equal(ct[sl], key.encrypt(m[sl], r[sl]))
+        assert np.array_equal(s[sl], key.add(ct[sl], ct2[sl]))
+        assert np.array_equal(ml[sl], key.mul(ct[sl], k[sl]))
+        assert np.array_equal(ez[sl], key.encrypt_zero(r[sl]))
+        assert np.array_equal(rz[sl], key.randomize(ct[sl], r[::-1][sl].copy()))
+        assert np.array_equal(ap[sl], key.add_plain(ct[sl], k[sl]))
+    d, _ = key.decrypt(ml)
+    assert np.array_equal(d, m * k)
+    bad = ct.copy()
+    bad[per + 7] = 0xFFFFFFFF  # >= n^2, in the chunk on the second lane
+    with pytest.raises(hg.HgError) as ei:
+        key.decrypt(bad)
+    assert ei.value.code == capi.HG_ERR_CT_RANGE
+    with pytest.raises(hg.HgError) as ei:
+        key.mul(bad, k)
+    assert ei.value.code == capi.HG_ERR_CT_RANGE
+    noinv = ct.copy()
+    noinv[per + 9] = key.to_mont(hg.ints_to_limbs([sk.p], key.ct_limbs))[0]
+    kneg = np.full(n, -3, dtype=np.int64)
+    with pytest.raises(hg.HgError) as ei:
+        key.mul(noinv, kneg)
+    assert ei.value.code == capi.HG_ERR_NOT_INVERTIBLE
+    d, _ = key.decrypt(key.mul(ct, kneg))
+    assert np.array_equal(d, -3 * m)
+
+
+def test_chunked_host_calls_from_threads(gpu_key):
+    """Chunked calls from several threads: each takes a second lane only when
+    one is free, so none waits on another."""
+    import threading
+
+    key, pk, sk = gpu_key(1024, 1)
+    errors = []
+
+    def worker(t):
+        try:
+            rng = np.random.default_rng(200 + t)
+            n = (1 << 17) + t
+            m = rng.integers(-(2 ** 50), 2 ** 50, size=n)
+            r = rng.integers(0, 2 ** 32, size=(n, key.r_limbs), dtype=np.uint64).astype(np.uint32)
+            d, ovf = key.decrypt(key.add(key.encrypt(m, r), key.encrypt(m, r)))
+            if not (ovf.sum() == 0 and np.array_equal(d, 2 * m)):
+                errors.append(t)
+        except Exception as e:  # collected for the main thread
+            errors.append(repr(e))
+
+    ths = [threading.Thread(target=worker, args=(t,)) for t in range(5)]
+    for t in ths:
+        t.start()
+    for t in ths:
+        t.join()
+    assert not errors, errors
