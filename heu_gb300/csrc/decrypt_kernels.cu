@@ -1,6 +1,7 @@
 // CRT decryption kernel (decryptor.cc:32-53): two groups of TP lanes per
 // ciphertext, one per prime; persistent grid, each unit slot owning two
-// odd-power tables in scratch and a hand-off buffer in shared memory.
+// odd-power tables in scratch and a hand-off buffer in shared memory; warps
+// take ciphertexts from a launch-wide counter (next_work).
 #include <algorithm>
 
 #include "paillier_ops.cuh"
@@ -18,7 +19,7 @@ __global__ void __launch_bounds__(kBlock) k_decrypt(KeyConst kc, SecConst sc, co
                                                     size_t count, int64_t* __restrict__ out_i64,
                                                     uint8_t* __restrict__ out_ovf, uint32_t* __restrict__ out_mag,
                                                     uint8_t* __restrict__ out_neg, uint32_t* __restrict__ scratch,
-                                                    uint32_t* err) {
+                                                    uint32_t* err, unsigned long long* ctr) {
   constexpr int SP = TP * LP;
   constexpr int UPW = 32 / (2 * TP);  // ciphertexts per warp
   constexpr int UPB = kBlock / (2 * TP);
@@ -28,11 +29,9 @@ __global__ void __launch_bounds__(kBlock) k_decrypt(KeyConst kc, SecConst sc, co
   const int side = (lane / TP) & 1;
   const int unit_w = lane / (2 * TP);
   const int unit_b = threadIdx.x / (2 * TP);
-  const int warp_first = (threadIdx.x >> 5) * UPW;
-  const size_t stride = (size_t)gridDim.x * UPB;
   const int ntab = 1 << (sc.wd - 1);
   uint32_t* tb = scratch + (((size_t)blockIdx.x * UPB + unit_b) * 2 + side) * (size_t)ntab * SP + g.t * LP;
-  for (size_t wbase = (size_t)blockIdx.x * UPB + warp_first; wbase < count; wbase += stride) {
+  for (size_t wbase = next_work(ctr, UPW); wbase < count; wbase = next_work(ctr, UPW)) {
     const size_t inst = wbase + unit_w;
     const bool active = inst < count;
     decrypt_one<TP, LP>(kc, sc, ct, active ? inst : count - 1, active, side, tb, ysm[unit_b], out_i64, out_ovf,
@@ -65,13 +64,16 @@ int resident_blocks_decrypt(int Sp, int variant) {
 
 cudaError_t launch_decrypt(int Sp, const KeyConst& kc, const SecConst& sc, const uint32_t* ct, size_t count,
                            int64_t* out_i64, uint8_t* out_ovf, uint32_t* out_mag, uint8_t* out_neg,
-                           uint32_t* scratch, uint32_t* err, int grid, cudaStream_t st) {
+                           uint32_t* scratch, uint32_t* err, int grid, unsigned long long* ctr, cudaStream_t st) {
   if (count == 0) return cudaSuccess;
+  const cudaError_t e = cudaMemsetAsync(ctr, 0, sizeof(*ctr), st);
+  if (e != cudaSuccess) return e;
   HG_DISPATCH_SPV(Sp, sc.variant, {
     const size_t upb = kBlock / (2 * TP);
     const unsigned need = (unsigned)((count + upb - 1) / upb);
     const unsigned gb = (unsigned)std::min((size_t)need, (size_t)grid);
-    k_decrypt<TP, LP><<<gb, kBlock, 0, st>>>(kc, sc, ct, count, out_i64, out_ovf, out_mag, out_neg, scratch, err);
+    k_decrypt<TP, LP><<<gb, kBlock, 0, st>>>(kc, sc, ct, count, out_i64, out_ovf, out_mag, out_neg, scratch, err,
+                                             ctr);
   });
   count_launches(1);
   return cudaGetLastError();

@@ -244,7 +244,9 @@ struct Work {
   ~Work() {
     if (own_stream && stream) cudaStreamDestroy(stream);
   }
+  DevBuf ctr;  // work counter of the persistent kernels this lane launches
   uint32_t* errp() { return err.ensure<uint32_t>(sizeof(uint32_t)); }
+  unsigned long long* ctrp() { return ctr.ensure<unsigned long long>(sizeof(unsigned long long)); }
 };
 
 }  // namespace
@@ -451,7 +453,7 @@ void core_decrypt(KeyRec& k, Work& w, const uint32_t* ct, int64_t* m, uint8_t* o
     const size_t units = (size_t)k.grid_oudec * k.upb_oudec;
     uint32_t* scratch = w.scratch.ensure<uint32_t>(units * ntab * k.oc.Sp * 4);
     cuda_check(hg::launch_ou_decrypt(k.S, k.kc, k.oc, ct, count, m, ovf, mag, neg, scratch, w.errp(), k.grid_oudec,
-                                     w.stream),
+                                     w.ctrp(), w.stream),
                "OU decrypt launch");
     return;
   }
@@ -459,7 +461,7 @@ void core_decrypt(KeyRec& k, Work& w, const uint32_t* ct, int64_t* m, uint8_t* o
   const size_t units = (size_t)k.grid_dec * hg::units_per_block_decrypt(k.Sp, k.sc.variant);
   uint32_t* scratch = w.scratch.ensure<uint32_t>(units * 2 * ntab * k.Sp * 4);
   cuda_check(hg::launch_decrypt(k.Sp, k.kc, k.sc, ct, count, m, ovf, mag, neg, scratch, w.errp(), k.grid_dec,
-                                w.stream),
+                                w.ctrp(), w.stream),
              "decrypt launch");
 }
 
@@ -544,7 +546,7 @@ void core_mul(KeyRec& k, Work& w, const uint32_t* a, const int64_t* kk, const in
   const size_t ntab = (size_t)1 << (k.wm - 1);
   const size_t inst = (size_t)k.grid_mul * hg::instances_per_block(k.S, k.kc.variant);
   uint32_t* scratch = w.scratch.ensure<uint32_t>(inst * ntab * k.S * 4);
-  cuda_check(hg::launch_mul(k.S, k.kc, a, kk, out, count, scratch, k.wm, w.errp(), k.grid_mul, w.stream),
+  cuda_check(hg::launch_mul(k.S, k.kc, a, kk, out, count, scratch, k.wm, w.errp(), k.grid_mul, w.ctrp(), w.stream),
              "mul launch");
   bool any_neg = true;
   if (host_k) {
@@ -1967,7 +1969,8 @@ int hg_autotune(hg_ctx* ctx, int key_id, size_t calib, hg_key_config* best, doub
         const double tm = timed([&] {
           const size_t inst = (size_t)k->grid_mul * hg::instances_per_block(k->S, k->kc.variant);
           uint32_t* scratch = w.scratch.ensure<uint32_t>(inst * ((size_t)1 << (k->wm - 1)) * k->S * 4);
-          cuda_check(hg::launch_mul(k->S, k->kc, dct, dk, dout, n, scratch, k->wm, w.errp(), k->grid_mul, w.stream),
+          cuda_check(hg::launch_mul(k->S, k->kc, dct, dk, dout, n, scratch, k->wm, w.errp(), k->grid_mul, w.ctrp(),
+                                    w.stream),
                      "mul launch");
         });
         if (te + tm < best_nn) {

@@ -91,7 +91,7 @@ __global__ void __launch_bounds__(kBlock) k_ou_decrypt(KeyConst kc, OuConst oc, 
                                                        size_t count, int64_t* __restrict__ out_i64,
                                                        uint8_t* __restrict__ out_ovf, uint32_t* __restrict__ out_mag,
                                                        uint8_t* __restrict__ out_neg, uint32_t* __restrict__ scratch,
-                                                       uint32_t* err) {
+                                                       uint32_t* err, unsigned long long* ctr) {
   constexpr int SP = TP * LP;
   static_assert(S <= 2 * SP, "ciphertext must fit the wide reduction");
   constexpr int UPW = 32 / TP;
@@ -101,13 +101,11 @@ __global__ void __launch_bounds__(kBlock) k_ou_decrypt(KeyConst kc, OuConst oc, 
   const int lane = threadIdx.x & 31;
   const int unit_w = lane / TP;
   const int unit_b = threadIdx.x / TP;
-  const int warp_first = (threadIdx.x >> 5) * UPW;
-  const size_t stride = (size_t)gridDim.x * UPB;
   const int ntab = 1 << (oc.wd - 1);
   uint32_t* tb = scratch + ((size_t)blockIdx.x * UPB + unit_b) * (size_t)ntab * SP + g.t * LP;
   uint32_t N[LP];
   load_slice<LP>(N, oc.P2 + g.t * LP);
-  for (size_t wbase = (size_t)blockIdx.x * UPB + warp_first; wbase < count; wbase += stride) {
+  for (size_t wbase = next_work(ctr, UPW); wbase < count; wbase = next_work(ctr, UPW)) {
     const size_t inst = wbase + unit_w;
     const bool active = inst < count;
     const size_t i = active ? inst : count - 1;
@@ -258,14 +256,17 @@ cudaError_t ou_decrypt_geometry(int S, int Sp, int* grid, int* units_per_block) 
 
 cudaError_t launch_ou_decrypt(int S, const KeyConst& kc, const OuConst& oc, const uint32_t* ct, size_t count,
                               int64_t* out_i64, uint8_t* out_ovf, uint32_t* out_mag, uint8_t* out_neg,
-                              uint32_t* scratch, uint32_t* err, int grid, cudaStream_t st) {
+                              uint32_t* scratch, uint32_t* err, int grid, unsigned long long* ctr,
+                              cudaStream_t st) {
   if (count == 0) return cudaSuccess;
+  const cudaError_t e = cudaMemsetAsync(ctr, 0, sizeof(*ctr), st);
+  if (e != cudaSuccess) return e;
   HG_DISPATCH_OU(S, oc.Sp, {
     const size_t upb = kBlock / TP;
     const unsigned need = (unsigned)((count + upb - 1) / upb);
     const unsigned gb = (unsigned)std::min((size_t)need, (size_t)grid);
     k_ou_decrypt<TP, LP, SC><<<gb, kBlock, 0, st>>>(kc, oc, ct, count, out_i64, out_ovf, out_mag, out_neg, scratch,
-                                                   err);
+                                                   err, ctr);
   });
   count_launches(1);
   return cudaGetLastError();

@@ -71,18 +71,18 @@ template <int TPI, int L>
 __global__ void __launch_bounds__(kBlock) k_mul(KeyConst kc, const uint32_t* __restrict__ a,
                                                 const int64_t* __restrict__ kk, uint32_t* __restrict__ out,
                                                 size_t count, uint32_t* __restrict__ scratch, int wm,
-                                                uint32_t* err) {
+                                                uint32_t* err, unsigned long long* ctr) {
   constexpr int S = TPI * L;
   constexpr int IPB = kBlock / TPI;
+  constexpr int IPW = 32 / TPI;
   const Group<TPI> g;
   const int lane_inst = (threadIdx.x & 31) / TPI;
-  const int warp_first = (threadIdx.x >> 5) * (32 / TPI);
-  const size_t stride = (size_t)gridDim.x * IPB;
+  const int warp_first = (threadIdx.x >> 5) * IPW;
   const int ntab = 1 << (wm - 1);
   uint32_t* tb = scratch + ((size_t)blockIdx.x * IPB + warp_first + lane_inst) * (size_t)ntab * S + g.t * L;
   uint32_t N[L];
   load_slice<L>(N, kc.N + g.t * L);
-  for (size_t wbase = (size_t)blockIdx.x * IPB + warp_first; wbase < count; wbase += stride) {
+  for (size_t wbase = next_work(ctr, IPW); wbase < count; wbase = next_work(ctr, IPW)) {
     const size_t inst = wbase + lane_inst;
     const bool active = inst < count;
     mul_one<TPI, L>(kc, a, kk, out, active ? inst : count - 1, active, tb, wm, N, g, err);
@@ -306,12 +306,15 @@ cudaError_t launch_add_plain(int S, const KeyConst& kc, const uint32_t* a, const
 }
 
 cudaError_t launch_mul(int S, const KeyConst& kc, const uint32_t* a, const int64_t* k, uint32_t* out,
-                       size_t count, uint32_t* scratch, int wm, uint32_t* err, int grid, cudaStream_t st) {
+                       size_t count, uint32_t* scratch, int wm, uint32_t* err, int grid, unsigned long long* ctr,
+                       cudaStream_t st) {
   if (count == 0) return cudaSuccess;
+  const cudaError_t e = cudaMemsetAsync(ctr, 0, sizeof(*ctr), st);
+  if (e != cudaSuccess) return e;
   HG_DISPATCH_SV(S, kc.variant, {
     const unsigned need = blocks_for(count, TPI);
     const unsigned gb = (unsigned)std::min((size_t)need, (size_t)grid);
-    k_mul<TPI, L><<<gb, kBlock, 0, st>>>(kc, a, k, out, count, scratch, wm, err);
+    k_mul<TPI, L><<<gb, kBlock, 0, st>>>(kc, a, k, out, count, scratch, wm, err, ctr);
   });
   return counted();
 }

@@ -83,16 +83,20 @@ cudaError_t launch_add(int S, const KeyConst& kc, const uint32_t* a, const uint3
                        size_t count, uint32_t* err, cudaStream_t st);
 cudaError_t launch_add_plain(int S, const KeyConst& kc, const uint32_t* a, const int64_t* p, int neg_p,
                              uint32_t* out, size_t count, uint32_t* err, cudaStream_t st);
+// The persistent kernels (mul, decrypt, OU decrypt) take work from *ctr, a
+// device counter that the launcher zeroes in stream order before the launch.
 cudaError_t launch_mul(int S, const KeyConst& kc, const uint32_t* a, const int64_t* k, uint32_t* out,
-                       size_t count, uint32_t* scratch, int wm, uint32_t* err, int grid, cudaStream_t st);
+                       size_t count, uint32_t* scratch, int wm, uint32_t* err, int grid, unsigned long long* ctr,
+                       cudaStream_t st);
 cudaError_t launch_decrypt(int Sp, const KeyConst& kc, const SecConst& sc, const uint32_t* ct, size_t count,
                            int64_t* out_i64, uint8_t* out_ovf, uint32_t* out_mag, uint8_t* out_neg,
-                           uint32_t* scratch, uint32_t* err, int grid, cudaStream_t st);
+                           uint32_t* scratch, uint32_t* err, int grid, unsigned long long* ctr, cudaStream_t st);
 // OU decryption over S-limb ciphertexts with Sp-limb p^2 arithmetic
 // (S, Sp) in {(64, 32), (128, 64), (128, 96)}.
 cudaError_t launch_ou_decrypt(int S, const KeyConst& kc, const OuConst& oc, const uint32_t* ct, size_t count,
                               int64_t* out_i64, uint8_t* out_ovf, uint32_t* out_mag, uint8_t* out_neg,
-                              uint32_t* scratch, uint32_t* err, int grid, cudaStream_t st);
+                              uint32_t* scratch, uint32_t* err, int grid, unsigned long long* ctr,
+                              cudaStream_t st);
 cudaError_t ou_decrypt_geometry(int S, int Sp, int* grid, int* units_per_block);
 // Signed plaintexts -> non-negative exponents for the G and G^-1 tables.
 cudaError_t launch_ou_split_i64(const int64_t* p, int negate, uint32_t* ep, uint32_t* en, size_t count,

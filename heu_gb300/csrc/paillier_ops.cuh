@@ -475,6 +475,16 @@ __device__ __forceinline__ void convert_one(const KeyConst& kc, const uint32_t* 
   if (active) store_slice<L>(out + i * S + g.t * L, A);
 }
 
+// The next `per_warp` work items for the calling warp, from a launch-wide
+// counter zeroed before the launch.  Persistent kernels take their work this
+// way rather than in fixed strided shares, so warps on faster SMs take more
+// and none idles while another still holds a static share.
+__device__ __forceinline__ size_t next_work(unsigned long long* ctr, int per_warp) {
+  unsigned long long v = 0;
+  if ((threadIdx.x & 31) == 0) v = atomicAdd(ctr, (unsigned long long)per_warp);
+  return (size_t)__shfl_sync(0xffffffffu, v, 0);
+}
+
 }  // namespace hg
 
 // ---------------------------------------------------------------------------
