@@ -78,6 +78,12 @@ SIGNATURES = {
     "hg_dev_negate": [_P, _I, _P, _P, _SZ, _P],
     "hg_dev_sum_noalloc": [_P, _I, _P, _SZ, _P, _P],
     "hg_dev_check": [_P],
+    "hg_serialize_bound": [_P, _I, _SZ, ctypes.POINTER(_SZ)],
+    "hg_serialize": [_P, _I, _P, _SZ, _SZ, _I, _I, _P, _SZ, ctypes.POINTER(_SZ)],
+    "hg_deserialize": [_P, _I, _P, _SZ, _I, _P, _SZ, ctypes.POINTER(_SZ), ctypes.POINTER(_SZ), ctypes.POINTER(_I)],
+    "hg_dev_serialize": [_P, _I, _P, _SZ, _SZ, _I, _I, _P, _SZ, ctypes.POINTER(_SZ), _P],
+    "hg_dev_deserialize": [_P, _I, _P, _SZ, _I, _P, _SZ, ctypes.POINTER(_SZ), ctypes.POINTER(_SZ),
+                           ctypes.POINTER(_I), _P],
     "hg_bucket_sum": [_P, _I, _P, _SZ, _SZ, _P, _SZ, _I, _I, _P],
     "hg_dev_bucket_sum": [_P, _I, _P, _SZ, _SZ, _P, _SZ, _I, _I, _P, _P],
     "hg_matmul": [_P, _I, _P, _SZ, _SZ, _P, _SZ, _P],

@@ -302,6 +302,7 @@ void reset_err(Work& w) { cuda_check(cudaMemsetAsync(w.errp(), 0, sizeof(uint32_
 void raise_err_bits(uint32_t bits) {
   if (bits & hg::kErrCtRange) fail(HG_ERR_CT_RANGE, "Invalid ciphertext: value >= n^2");
   if (bits & hg::kErrBinRange) fail(HG_ERR_INVALID, "order map holds a bin id >= bucket_num");
+  if (bits & hg::kErrFormat) fail(HG_ERR_INVALID, "Cannot parse inner_obj: buffer format error (ciphertext item)");
   if (bits & hg::kErrPtRange) fail(HG_ERR_PT_RANGE, "message number out of range: |m| > n/2");
   if (bits & hg::kErrNotInvertible) fail(HG_ERR_NOT_INVERTIBLE, "ciphertext not invertible mod n^2");
 }
@@ -1420,6 +1421,284 @@ int hg_mul(hg_ctx* ctx, int key_id, const uint32_t* a, const int64_t* kk, uint32
       core_mul(*k, v, da, dk, kk + off, dout, cnt, false);
       d2h((uint8_t*)out + off * cb, dout, cnt * cb, v);
     }, [](Work& v) { v.task.status = 0; }, [](Work& v) { raise_task_status(v.task); });
+    return HG_OK;
+  });
+}
+
+// ---------------------------------------------------------------------------
+// HEU wire format for ciphertext matrices (numpy/matrix.h:221-310); the items
+// are packed and unpacked by the kernels in wire_kernels.cu, the msgpack
+// headers around them are written and walked here.
+// ---------------------------------------------------------------------------
+static Work& dev_work(hg_ctx* ctx, void* stream);
+
+namespace {
+
+// SchemaType values (phe/base/schema.h:47-51) appended to every item.
+uint64_t schema_value(const KeyRec& k) { return k.scheme == 1 ? 1u : 4u; }
+
+void mp_uint(std::vector<uint8_t>& h, uint64_t v) {  // msgpack-c's smallest form of a non-negative int
+  auto be = [&](int n) {
+    for (int i = n - 1; i >= 0; --i) h.push_back((uint8_t)(v >> (8 * i)));
+  };
+  if (v < 128u) {
+    h.push_back((uint8_t)v);
+  } else if (v < 256u) {
+    h.push_back(0xcc);
+    be(1);
+  } else if (v < 65536u) {
+    h.push_back(0xcd);
+    be(2);
+  } else if (v < (1ull << 32)) {
+    h.push_back(0xce);
+    be(4);
+  } else {
+    h.push_back(0xcf);
+    be(8);
+  }
+}
+
+// fixarray(4), rows, cols, ndim, then the array header of the items
+std::vector<uint8_t> wire_prefix(size_t rows, size_t cols, int ndim) {
+  std::vector<uint8_t> h{0x94};
+  mp_uint(h, rows);
+  mp_uint(h, cols);
+  mp_uint(h, (uint64_t)ndim);
+  const uint64_t n = (uint64_t)rows * cols;
+  if (n < 16u) {
+    h.push_back((uint8_t)(0x90u | n));
+  } else if (n < 65536u) {
+    h.push_back(0xdc);
+    h.push_back((uint8_t)(n >> 8));
+    h.push_back((uint8_t)n);
+  } else {
+    h.push_back(0xdd);
+    for (int i = 3; i >= 0; --i) h.push_back((uint8_t)(n >> (8 * i)));
+  }
+  return h;
+}
+
+struct WireReader {
+  const uint8_t* p;
+  size_t n, i = 0;
+  [[noreturn]] void bad(const char* what) const {
+    fail(HG_ERR_INVALID, std::string("Cannot parse: buffer format error (") + what + ")");
+  }
+  uint64_t be(int k) {
+    if (n - i < (size_t)k) bad("truncated");
+    uint64_t v = 0;
+    for (int j = 0; j < k; ++j) v = (v << 8) | p[i++];
+    return v;
+  }
+  uint8_t byte() { return (uint8_t)be(1); }
+  int64_t integer() {
+    const uint8_t t = byte();
+    if (t < 0x80) return t;
+    if (t >= 0xe0) return (int8_t)t;
+    switch (t) {
+      case 0xcc: return (int64_t)be(1);
+      case 0xcd: return (int64_t)be(2);
+      case 0xce: return (int64_t)be(4);
+      case 0xcf: {
+        const uint64_t v = be(8);
+        if (v > (uint64_t)INT64_MAX) bad("integer");
+        return (int64_t)v;
+      }
+      case 0xd0: return (int8_t)be(1);
+      case 0xd1: return (int16_t)be(2);
+      case 0xd2: return (int32_t)be(4);
+      case 0xd3: return (int64_t)be(8);
+      default: bad("integer");
+    }
+  }
+  uint64_t array() {
+    const uint8_t t = byte();
+    if ((t & 0xf0) == 0x90) return t & 0x0f;
+    if (t == 0xdc) return be(2);
+    if (t == 0xdd) return be(4);
+    bad("array");
+  }
+  // str or bin (msgpack-c's as<std::string_view> takes both)
+  uint64_t bytes() {
+    const uint8_t t = byte();
+    if ((t & 0xe0) == 0xa0) return t & 0x1f;
+    if (t == 0xd9 || t == 0xc4) return be(1);
+    if (t == 0xda || t == 0xc5) return be(2);
+    if (t == 0xdb || t == 0xc6) return be(4);
+    bad("item");
+  }
+};
+
+struct WireIndex {
+  size_t rows = 0, cols = 0;
+  int ndim = 0;
+  std::vector<uint64_t> offs, lens;
+};
+
+// The host walk: header checks of matrix.h:280-292, one offset per item.
+WireIndex wire_walk(const uint8_t* buf, size_t len) {
+  WireReader r{buf, len};
+  WireIndex w;
+  if (r.array() != 4) r.bad("not a 4-element array");
+  const int64_t rows = r.integer(), cols = r.integer(), ndim = r.integer();
+  if (rows < 0 || cols < 0 || ndim < 0 || ndim > 2) r.bad("shape");
+  w.rows = (size_t)rows;
+  w.cols = (size_t)cols;
+  w.ndim = (int)ndim;
+  const uint64_t n = r.array();
+  if ((unsigned __int128)n != (unsigned __int128)(uint64_t)rows * (uint64_t)cols)
+    r.bad("inner array size != rows * cols");
+  if (n > len - r.i) r.bad("truncated");  // every item takes at least one byte
+  w.offs.resize(n);
+  w.lens.resize(n);
+  for (uint64_t k = 0; k < n; ++k) {
+    const uint64_t l = r.bytes();
+    if (len - r.i < l) r.bad("truncated item");
+    w.offs[k] = r.i;
+    w.lens[k] = l;
+    r.i += l;
+  }
+  return w;
+}
+
+void wire_pack(KeyRec& k, Work& w, const uint32_t* dct, size_t rows, size_t cols, int row_major,
+               const std::vector<uint8_t>& prefix, uint8_t* host_out, uint8_t* dev_out, size_t cap, size_t* len) {
+  const size_t count = rows * cols;
+  auto* mag = w.io[1].ensure<uint32_t>(std::max<size_t>(count, 1) * 4);
+  auto* scr = w.io[2].ensure<uint64_t>(hg::wire_scratch_words(count) * 8);
+  auto* tot = w.io[3].ensure<uint64_t>(8);
+  cuda_check(hg::launch_wire_size(dct, rows, cols, row_major, k.S, mag, scr, tot, w.stream), "wire size");
+  uint64_t* htot = w.pin_err.ensure<uint64_t>(8);
+  cuda_check(cudaMemcpyAsync(htot, tot, 8, cudaMemcpyDeviceToHost, w.stream), "D2H total");
+  cuda_check(cudaStreamSynchronize(w.stream), "stream sync");
+  const size_t need = prefix.size() + (size_t)*htot;
+  *len = need;
+  if (need > cap) fail(HG_ERR_INVALID, "output buffer too small: " + std::to_string(need) + " bytes needed");
+  if (dev_out) {
+    cuda_check(cudaMemcpyAsync(dev_out, prefix.data(), prefix.size(), cudaMemcpyHostToDevice, w.stream), "H2D prefix");
+    cuda_check(hg::launch_wire_write(dct, rows, cols, row_major, k.S, schema_value(k), mag, scr, dev_out, prefix.size(),
+                                     w.stream),
+               "wire write");
+  } else {
+    std::memcpy(host_out, prefix.data(), prefix.size());
+    auto* dbytes = w.io[4].ensure<uint8_t>(std::max<size_t>((size_t)*htot, 1));
+    cuda_check(hg::launch_wire_write(dct, rows, cols, row_major, k.S, schema_value(k), mag, scr, dbytes, 0, w.stream),
+               "wire write");
+    d2h(host_out + prefix.size(), dbytes, (size_t)*htot, w);
+  }
+}
+
+void wire_unpack(KeyRec& k, Work& w, const uint8_t* buf, const WireIndex& ix, int row_major, uint32_t* dout) {
+  const size_t n = ix.offs.size();
+  if (n == 0) return;
+  // the items span [first offset, end of the last item)
+  const size_t lo = (size_t)ix.offs.front(), hi = (size_t)(ix.offs.back() + ix.lens.back());
+  auto* dbuf = w.io[1].ensure<uint8_t>(hi - lo);
+  auto* doffs = w.io[2].ensure<uint64_t>(n * 8);
+  auto* dlens = w.io[3].ensure<uint64_t>(n * 8);
+  std::vector<uint64_t> rel(n);
+  for (size_t i = 0; i < n; ++i) rel[i] = ix.offs[i] - lo;
+  h2d(dbuf, buf + lo, hi - lo, w);
+  h2d(doffs, rel.data(), n * 8, w);
+  h2d(dlens, ix.lens.data(), n * 8, w);
+  cuda_check(hg::launch_wire_unpack(dbuf, doffs, dlens, ix.rows, ix.cols, row_major, k.S, schema_value(k), dout,
+                                     w.errp(), w.stream),
+             "wire read");
+  // rel and the index must outlive the copies: the caller synchronises
+  cuda_check(cudaStreamSynchronize(w.stream), "stream sync");
+}
+
+}  // namespace
+
+int hg_serialize_bound(hg_ctx* ctx, int key_id, size_t count, size_t* bytes) {
+  return guarded(__func__, [&] {
+    if (!bytes) fail(HG_ERR_INVALID, "null argument");
+    KeyRec* k = get_key(ctx, key_id);
+    // header <= 1 + 3 * 9 + 5; item <= str32 + fixarray + bin32 + 4S + 8
+    *bytes = 33 + count * (5 + 1 + 5 + (size_t)k->S * 4 + 8);
+    return HG_OK;
+  });
+}
+
+int hg_serialize(hg_ctx* ctx, int key_id, const uint32_t* ct, size_t rows, size_t cols, int ndim, int row_major,
+                 uint8_t* out, size_t cap, size_t* len) {
+  return guarded(__func__, [&] {
+    if (!out || !len || (!ct && rows * cols)) fail(HG_ERR_INVALID, "null argument");
+    if (ndim < 0 || ndim > 2) fail(HG_ERR_INVALID, "ndim must be 0, 1 or 2");
+    if (cols && rows > SIZE_MAX / cols) fail(HG_ERR_INVALID, "rows * cols overflows");
+    KeyRec* k = get_key(ctx, key_id);
+    set_device(ctx);
+    LaneGuard lane(ctx);
+    Work& w = *lane.w;
+    reset_err(w);
+    const size_t count = rows * cols, cb = ct_bytes(*k);
+    auto* dct = w.io[0].ensure<uint32_t>(std::max<size_t>(count, 1) * cb);
+    h2d(dct, ct, count * cb, w);
+    wire_pack(*k, w, dct, rows, cols, row_major, wire_prefix(rows, cols, ndim), out, nullptr, cap, len);
+    finish(w);
+    return HG_OK;
+  });
+}
+
+int hg_dev_serialize(hg_ctx* ctx, int key_id, const uint32_t* ct, size_t rows, size_t cols, int ndim, int row_major,
+                     uint8_t* out, size_t cap, size_t* len, void* stream) {
+  return guarded(__func__, [&] {
+    if (!out || !len || (!ct && rows * cols)) fail(HG_ERR_INVALID, "null argument");
+    if (ndim < 0 || ndim > 2) fail(HG_ERR_INVALID, "ndim must be 0, 1 or 2");
+    if (cols && rows > SIZE_MAX / cols) fail(HG_ERR_INVALID, "rows * cols overflows");
+    KeyRec* k = get_key(ctx, key_id);
+    set_device(ctx);
+    Work& w = dev_work(ctx, stream);
+    wire_pack(*k, w, ct, rows, cols, row_major, wire_prefix(rows, cols, ndim), nullptr, out, cap, len);
+    cuda_check(cudaStreamSynchronize(w.stream), "stream sync");
+    return HG_OK;
+  });
+}
+
+int hg_deserialize(hg_ctx* ctx, int key_id, const uint8_t* buf, size_t len, int row_major, uint32_t* ct_out,
+                   size_t cap_count, size_t* rows, size_t* cols, int* ndim) {
+  return guarded(__func__, [&] {
+    if (!buf || !rows || !cols || !ndim) fail(HG_ERR_INVALID, "null argument");
+    KeyRec* k = get_key(ctx, key_id);
+    const WireIndex ix = wire_walk(buf, len);
+    const size_t n = ix.offs.size();
+    *rows = ix.rows;
+    *cols = ix.cols;
+    *ndim = ix.ndim;
+    if (n > cap_count) fail(HG_ERR_INVALID, "output holds " + std::to_string(cap_count) + " ciphertexts, " +
+                                                std::to_string(n) + " serialized");
+    if (n && !ct_out) fail(HG_ERR_INVALID, "null argument");
+    if (n == 0) return HG_OK;
+    set_device(ctx);
+    LaneGuard lane(ctx);
+    Work& w = *lane.w;
+    reset_err(w);
+    const size_t cb = ct_bytes(*k);
+    auto* dout = w.io[0].ensure<uint32_t>(n * cb);
+    wire_unpack(*k, w, buf, ix, row_major, dout);
+    d2h(ct_out, dout, n * cb, w);
+    finish(w);
+    return HG_OK;
+  });
+}
+
+int hg_dev_deserialize(hg_ctx* ctx, int key_id, const uint8_t* buf, size_t len, int row_major, uint32_t* ct_out,
+                       size_t cap_count, size_t* rows, size_t* cols, int* ndim, void* stream) {
+  return guarded(__func__, [&] {
+    if (!buf || !rows || !cols || !ndim) fail(HG_ERR_INVALID, "null argument");
+    KeyRec* k = get_key(ctx, key_id);
+    const WireIndex ix = wire_walk(buf, len);
+    const size_t n = ix.offs.size();
+    *rows = ix.rows;
+    *cols = ix.cols;
+    *ndim = ix.ndim;
+    if (n > cap_count) fail(HG_ERR_INVALID, "output holds " + std::to_string(cap_count) + " ciphertexts, " +
+                                                std::to_string(n) + " serialized");
+    if (n && !ct_out) fail(HG_ERR_INVALID, "null argument");
+    if (n == 0) return HG_OK;
+    set_device(ctx);
+    Work& w = dev_work(ctx, stream);
+    wire_unpack(*k, w, buf, ix, row_major, ct_out);
     return HG_OK;
   });
 }

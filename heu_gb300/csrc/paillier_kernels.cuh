@@ -13,6 +13,7 @@ enum : uint32_t {
   kErrNotInvertible = 2u,
   kErrPtRange = 4u,      // a plaintext with |m| > n/2
   kErrBinRange = 8u,     // an order-map bin id >= bucket_num
+  kErrFormat = 16u,      // a serialized ciphertext item that does not parse
 };
 
 // Public-key constants for arithmetic mod N = n^2 with R = 2^(32*S).
@@ -154,5 +155,22 @@ int units_per_block_decrypt(int Sp, int variant);
 bool supported_limbs(int S);
 uint64_t launch_count();  // kernels launched by this process so far
 void count_launches(uint64_t n);
+
+// HEU wire format (wire_kernels.cu), over a rows x cols matrix whose items
+// are written in column-major order; row_major says how ct / out hold the
+// elements.  launch_wire_size fills mag_bytes (rows * cols words) and scratch
+// (wire_scratch_words(rows * cols) uint64 words: item offsets, block totals)
+// and copies the items' total bytes to *total_dev; launch_wire_write then
+// writes the items at out + base.  Unpacking: item k is
+// buf[offs[k] .. offs[k] + lens[k]).
+size_t wire_scratch_words(size_t count);
+cudaError_t launch_wire_size(const uint32_t* ct, size_t rows, size_t cols, int row_major, int S, uint32_t* mag_bytes,
+                             uint64_t* scratch, uint64_t* total_dev, cudaStream_t st);
+cudaError_t launch_wire_write(const uint32_t* ct, size_t rows, size_t cols, int row_major, int S, uint64_t schema,
+                              const uint32_t* mag_bytes, const uint64_t* scratch, uint8_t* out, size_t base,
+                              cudaStream_t st);
+cudaError_t launch_wire_unpack(const uint8_t* buf, const uint64_t* offs, const uint64_t* lens, size_t rows,
+                               size_t cols, int row_major, int S, uint64_t schema, uint32_t* out, uint32_t* err,
+                               cudaStream_t st);
 
 }  // namespace hg

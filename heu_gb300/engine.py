@@ -72,6 +72,22 @@ def ou_sizes(key_bits):
     raise ValueError("OU keys of 1024, 2048 or 3072 bits")
 
 
+def matrix_dims(shape):
+    """NumPy shape -> (rows, cols, ndim) of heu.numpy's DenseMatrix: a scalar
+    is 1 x 1, a vector n x 1 (numpy/shape.h:44-54)."""
+    if len(shape) == 0:
+        return 1, 1, 0
+    if len(shape) == 1:
+        return int(shape[0]), 1, 1
+    if len(shape) == 2:
+        return int(shape[0]), int(shape[1]), 2
+    raise ValueError("HEU tensor dimension cannot exceed 2")
+
+
+def numpy_shape(rows, cols, ndim):
+    return () if ndim == 0 else (rows,) if ndim == 1 else (rows, cols)
+
+
 def ou_random_bits(n_bits):
     """Bit length of OU encryption randomness for an n of n_bits bits
     (ou/encryptor.cc:12-20 with ou/public_key.h:27-31): 80 / 110 / 128."""
@@ -279,6 +295,36 @@ class Key:
         out = self._out(a.shape[0])
         capi.check(self.lib.hg_negate(self.ctx.handle, self.id, _ptr(a), _ptr(out), a.shape[0]))
         return out
+
+    # -- HEU wire format (numpy/matrix.h:221-310) --------------------------
+    def serialize(self, ct, shape=None):
+        """Ciphertexts in C order with NumPy shape `shape` (default: a vector)
+        -> the bytes of DenseMatrix<Ciphertext>::Serialize."""
+        ct = self._ct(ct)
+        shape = tuple(shape) if shape is not None else (ct.shape[0],)
+        rows, cols, ndim = matrix_dims(shape)
+        if rows * cols != ct.shape[0]:
+            raise ValueError(f"shape {shape} does not hold {ct.shape[0]} ciphertexts")
+        bound = ctypes.c_size_t()
+        capi.check(self.lib.hg_serialize_bound(self.ctx.handle, self.id, ct.shape[0], ctypes.byref(bound)))
+        out = np.empty(max(bound.value, 1), np.uint8)
+        n = ctypes.c_size_t()
+        capi.check(self.lib.hg_serialize(self.ctx.handle, self.id, _ptr(ct), rows, cols, ndim, 1, _ptr(out), out.size,
+                                         ctypes.byref(n)))
+        return out[:n.value].tobytes()
+
+    def deserialize(self, buf):
+        """DenseMatrix<Ciphertext>::LoadFrom -> (limbs in C order, NumPy shape)."""
+        b = np.frombuffer(buf, dtype=np.uint8)
+        rows, cols, ndim = ctypes.c_size_t(), ctypes.c_size_t(), ctypes.c_int()
+        args = (self.ctx.handle, self.id, _ptr(b), b.size, 1)
+        shp = (ctypes.byref(rows), ctypes.byref(cols), ctypes.byref(ndim))
+        rc = self.lib.hg_deserialize(*args, None, 0, *shp)
+        if rc != capi.HG_OK and rows.value * cols.value == 0:
+            capi.check(rc)
+        out = self._out(rows.value * cols.value)
+        capi.check(self.lib.hg_deserialize(*args, _ptr(out), out.shape[0], *shp))
+        return out, numpy_shape(rows.value, cols.value, ndim.value)
 
     def sum(self, a):
         a = self._ct(a)

@@ -101,6 +101,19 @@ class CiphertextArray:
 
     __repr__ = __str__
 
+    def serialize(self):
+        """DenseMatrix::Serialize (numpy/matrix.h:221-262, pylib ``serialize``):
+        HEU's msgpack layout, packed on the GPU."""
+        return self.kit.key.serialize(self.limbs, self.shape)
+
+    @staticmethod
+    def load_from(bytes_buffer, kit):
+        """DenseMatrix::LoadFrom (numpy/matrix.h:264-310, pylib ``load_from``).
+        Unlike the reference, the items are turned back into limbs by the
+        engine of ``kit``'s key, so the kit is an argument."""
+        limbs, shape = kit.key.deserialize(bytes_buffer)
+        return CiphertextArray(kit, limbs, shape)
+
 
 class BatchEncoder:
     """Two integers per plaintext (phe/encoding/batch_encoder.h:27-140):

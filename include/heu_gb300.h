@@ -309,6 +309,45 @@ int hg_dev_matmul(hg_ctx* ctx, int key_id, const uint32_t* x, size_t M, size_t K
                   uint32_t* out, void* stream);
 int hg_dev_check(hg_ctx* ctx);
 
+/* ---- HEU wire format of ciphertext matrices ---------------------------------
+ * Replaces DenseMatrix<Ciphertext>::Serialize / LoadFrom
+ * (heu/library/numpy/matrix.h:221-310, bound to Python as serialize /
+ * load_from and pickling in pylib/numpy_binding/bind_numpy.cc:42-59).
+ * Layout: msgpack [rows, cols, ndim, [item_0 .. item_{n-1}]], items as msgpack
+ * str; an item is msgpack [c] (MSGPACK_DEFINE(c_), paillier_zahlen/
+ * ciphertext.h:38, ou/ciphertext.h:38) followed by the schema value as a
+ * little-endian size_t (phe/base/serializable_types.cc:49-69): 4 = ZPaillier,
+ * 1 = OU (phe/base/schema.h:47-51).  c is the ciphertext's Montgomery-form
+ * value (the bytes the other calls exchange) as a msgpack bin of its
+ * little-endian magnitude without leading zero bytes.
+ * The items are in DenseMatrix's column-major order (matrix.h:159-162);
+ * row_major = 1 says ct / ct_out hold the matrix in C (row-major) order, as
+ * NumPy arrays do, and the kernels reorder; 0 = column-major as stored.
+ * ndim is 0, 1 or 2 (a scalar is 1 x 1, a vector n x 1).
+ * hg_serialize_bound gives an upper bound of the bytes; *len receives the
+ * exact size, and when it exceeds cap the call fails with HG_ERR_INVALID
+ * (nothing written) and *len still holds the size needed.
+ * hg_deserialize checks the structure (matrix.h:280-292: a 4-element array,
+ * inner array size = rows * cols) on the host, then unpacks the items on the
+ * GPU; an item that does not parse, whose value needs more than S limbs or
+ * whose schema value is not the key's fails with HG_ERR_INVALID.  When the
+ * matrix holds more than cap_count ciphertexts the call fails with
+ * HG_ERR_INVALID after setting *rows, *cols and *ndim (call with
+ * cap_count = 0 to learn the shape).
+ * The hg_dev_ forms take device ct / out (serialize) or a HOST buffer and a
+ * device ct_out (deserialize, e.g. bytes received from a peer); both
+ * synchronise `stream`; item errors of hg_dev_deserialize are reported by
+ * hg_dev_check. */
+int hg_serialize_bound(hg_ctx* ctx, int key_id, size_t count, size_t* bytes);
+int hg_serialize(hg_ctx* ctx, int key_id, const uint32_t* ct, size_t rows, size_t cols, int ndim, int row_major,
+                 uint8_t* out, size_t cap, size_t* len);
+int hg_deserialize(hg_ctx* ctx, int key_id, const uint8_t* buf, size_t len, int row_major, uint32_t* ct_out,
+                   size_t cap_count, size_t* rows, size_t* cols, int* ndim);
+int hg_dev_serialize(hg_ctx* ctx, int key_id, const uint32_t* ct, size_t rows, size_t cols, int ndim, int row_major,
+                     uint8_t* out, size_t cap, size_t* len, void* stream);
+int hg_dev_deserialize(hg_ctx* ctx, int key_id, const uint8_t* buf, size_t len, int row_major, uint32_t* ct_out,
+                       size_t cap_count, size_t* rows, size_t* cols, int* ndim, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
