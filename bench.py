@@ -881,6 +881,139 @@ def ou_arm(args):
     return 0
 
 
+def wire_arm(args):
+    """HEU wire format (numpy/matrix.h Serialize / LoadFrom) of 2^20
+    ciphertexts of a 2048-bit key: GPU pack from device ciphertexts to device
+    bytes, and load from host bytes (as received from a peer) to device
+    ciphertexts; the host-buffer round trip as e2e; the wire oracle on one
+    host core as the CPU baseline.  Roofline: algorithmic HBM bytes of a pack
+    (ciphertexts read once, items written once) over the pack's device time."""
+    import numpy as np
+    import torch
+
+    import heu_gb300 as hg
+    import heu_gb300.engine as eng
+    from heu_gb300 import capi
+
+    dev = torch.device("cuda", 0)
+    kp = eng.keygen(KEY_BITS, KEY_SEED)
+    ctx = hg.Context(0)
+    key = ctx.load_key(KEY_BITS, kp["n"], kp["h_s"], kp["p"], kp["q"], table_window=12)
+    lib, h = ctx.lib, ctx.handle
+    n, S = args.n, key.ct_limbs
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(31)
+    m = torch.randint(-(2 ** M_BITS), 2 ** M_BITS, (n,), dtype=torch.int64, device=dev, generator=gen)
+    r = torch.randint(-(2 ** 31), 2 ** 31, (n, key.r_limbs), dtype=torch.int32, device=dev, generator=gen)
+    ct = torch.empty((n, S), dtype=torch.int32, device=dev)
+    back = torch.empty_like(ct)
+    st = torch.cuda.Stream(device=dev)
+    sp = ctypes.c_void_p(st.cuda_stream)
+
+    def P(t):
+        return ctypes.c_void_p(t.data_ptr())
+
+    with torch.cuda.stream(st):
+        capi.check(lib.hg_dev_encrypt(h, key.id, P(m), P(r), P(ct), n, sp))
+    torch.cuda.synchronize()
+    bound = ctypes.c_size_t()
+    capi.check(lib.hg_serialize_bound(h, key.id, n, ctypes.byref(bound)))
+    dbuf = torch.empty(bound.value, dtype=torch.uint8, device=dev)
+    ln = ctypes.c_size_t()
+    rows, cols, nd = ctypes.c_size_t(), ctypes.c_size_t(), ctypes.c_int()
+
+    def pack():
+        capi.check(lib.hg_dev_serialize(h, key.id, P(ct), n, 1, 1, 1, P(dbuf), bound.value, ctypes.byref(ln), sp))
+
+    pack()
+    hbuf = dbuf[:ln.value].cpu().pin_memory()
+
+    def load():
+        capi.check(lib.hg_dev_deserialize(h, key.id, P(hbuf), hbuf.numel(), 1, P(back), n, ctypes.byref(rows),
+                                          ctypes.byref(cols), ctypes.byref(nd), sp))
+
+    for _ in range(args.warmup):
+        pack()
+        load()
+    torch.cuda.synchronize()
+    capi.check(lib.hg_dev_check(h))
+    clk = ClockSampler(0)
+    clk.start()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    t_pack = t_load = 0.0
+    for _ in range(args.steps):
+        ev[0].record(st)
+        pack()
+        ev[1].record(st)
+        load()
+        ev[2].record(st)
+        torch.cuda.synchronize()
+        t_pack += ev[0].elapsed_time(ev[1]) / 1e3
+        t_load += ev[1].elapsed_time(ev[2]) / 1e3
+    clocks = clk.stop()
+    capi.check(lib.hg_dev_check(h))
+    assert torch.equal(back, ct), "wire round trip mismatch"
+    t_pack /= args.steps
+    t_load /= args.steps
+    nbytes = ln.value
+    # e2e: host ciphertexts -> host bytes -> host ciphertexts through the C-ABI host-pointer calls
+    ct_pin = ct.cpu().pin_memory()
+    out_pin = torch.empty(bound.value, dtype=torch.uint8).pin_memory()
+    back_pin = torch.empty_like(ct_pin).pin_memory()
+
+    def e2e_step():
+        capi.check(lib.hg_serialize(h, key.id, P(ct_pin), n, 1, 1, 1, P(out_pin), bound.value, ctypes.byref(ln)))
+        capi.check(lib.hg_deserialize(h, key.id, P(out_pin), ln.value, 1, P(back_pin), n, ctypes.byref(rows),
+                                      ctypes.byref(cols), ctypes.byref(nd)))
+
+    e2e_step()
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    t_e2e = (time.perf_counter() - t) / args.steps
+    assert torch.equal(back_pin, ct_pin)
+    ct_h = ct_pin.numpy().view(np.uint32)
+    # the wire oracle on one core, bounded sample
+    from oracle import wire
+
+    ns = min(n, 1 << 15)
+    vals = hg.limbs_to_ints(ct_h[:ns])
+    t = time.perf_counter()
+    ob = wire.serialize_matrix(vals, ns, 1, 1, wire.SCHEMA_ZPAILLIER)
+    t_os = time.perf_counter() - t
+    t = time.perf_counter()
+    parsed = wire.parse_matrix(ob)
+    t_ol = time.perf_counter() - t
+    assert parsed[3] == vals
+    algo = n * S * 4 + nbytes  # algorithmic: ciphertexts read once, items written once
+    peak = None
+    try:
+        peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]
+    except (OSError, ValueError, KeyError):
+        peak = 6800.0
+    line = {
+        "metric": "HEU wire format ciphertexts/s (serialize + load, 2048-bit)", "value": n / (t_pack + t_load),
+        "unit": "ciphertexts/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": (t_pack + t_load) * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u8", "data": "synthetic",
+        "config": {"workload": "wire: 2^20 ciphertexts of a 2048-bit key, DenseMatrix msgpack layout, "
+                               "pack device->device, load host bytes->device", "bytes": nbytes},
+        "per_op_ciphertexts_per_s": {"serialize": n / t_pack, "load": n / t_load},
+        "roofline": {"bound": "hbm", "kernel": "serialize (k_wire_sizes + scan + k_wire_write)",
+                     "achieved": algo / t_pack / 1e9, "peak": peak, "unit": "GB/s",
+                     "frac": algo / t_pack / 1e9 / peak, "traffic": None,
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
+        "e2e": {"value": n / t_e2e, "unit": "ciphertexts/s", "h2d_bytes_per_step": n * S * 4 + nbytes,
+                "d2h_bytes_per_step": nbytes + n * S * 4, "api": "hg_serialize + hg_deserialize (host buffers)"},
+        "cpu_baseline": {"value": ns / (t_os + t_ol), "unit": "ciphertexts/s", "cores": 1, "kind": "port",
+                         "sample": f"wire oracle (Python) serialize + parse of {ns} ciphertexts, one core"},
+        "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+    ctx.close()
+    return 0
+
+
 def c5_arm(args):
     """Config 5: served request stream.  8 resident keypairs (six 2048-bit,
     two 3072-bit), Poisson arrivals at swept rates, lengths log-uniform in
@@ -1039,11 +1172,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=1 << 20)
-    ap.add_argument("--window", type=int, default=16)
+    ap.add_argument("--window", type=int, default=20)
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", choices=["config2", "config3", "config4", "config5", "ou"], default="config2")
+    ap.add_argument("--workload", choices=["config2", "config3", "config4", "config5", "ou", "wire"],
+                    default="config2")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner")
     ap.add_argument("--key-config", default=None,
                     help="explicit key config instead of the autotuner, e.g. "
@@ -1070,6 +1204,8 @@ def main():
         return c5_arm(args)
     if args.workload == "ou":
         return ou_arm(args)
+    if args.workload == "wire":
+        return wire_arm(args)
     return ours_arm(args)
 
 

@@ -25,6 +25,7 @@
 #include "batch.cuh"
 #include "engine_internal.hpp"
 #include "host_bn.hpp"
+#include "wire_host.hpp"
 #include "paillier_kernels.cuh"
 
 namespace {
@@ -239,7 +240,7 @@ struct Work {
   DevBuf mm_tables, mm_masks, mm_prod;
   DevBuf ou_e[2];
   DevBuf err;
-  PinBuf pin_root, pin_err, pin_z;
+  PinBuf pin_root, pin_err, pin_z, pin_wire;
   InvTask task;
   ~Work() {
     if (own_stream && stream) cudaStreamDestroy(stream);
@@ -1434,132 +1435,14 @@ static Work& dev_work(hg_ctx* ctx, void* stream);
 
 namespace {
 
+using hg::wire::WireReader;
+using hg::wire::WireShape;
+using hg::wire::wire_header;
+using hg::wire::wire_items;
+using hg::wire::wire_prefix;
+
 // SchemaType values (phe/base/schema.h:47-51) appended to every item.
 uint64_t schema_value(const KeyRec& k) { return k.scheme == 1 ? 1u : 4u; }
-
-void mp_uint(std::vector<uint8_t>& h, uint64_t v) {  // msgpack-c's smallest form of a non-negative int
-  auto be = [&](int n) {
-    for (int i = n - 1; i >= 0; --i) h.push_back((uint8_t)(v >> (8 * i)));
-  };
-  if (v < 128u) {
-    h.push_back((uint8_t)v);
-  } else if (v < 256u) {
-    h.push_back(0xcc);
-    be(1);
-  } else if (v < 65536u) {
-    h.push_back(0xcd);
-    be(2);
-  } else if (v < (1ull << 32)) {
-    h.push_back(0xce);
-    be(4);
-  } else {
-    h.push_back(0xcf);
-    be(8);
-  }
-}
-
-// fixarray(4), rows, cols, ndim, then the array header of the items
-std::vector<uint8_t> wire_prefix(size_t rows, size_t cols, int ndim) {
-  std::vector<uint8_t> h{0x94};
-  mp_uint(h, rows);
-  mp_uint(h, cols);
-  mp_uint(h, (uint64_t)ndim);
-  const uint64_t n = (uint64_t)rows * cols;
-  if (n < 16u) {
-    h.push_back((uint8_t)(0x90u | n));
-  } else if (n < 65536u) {
-    h.push_back(0xdc);
-    h.push_back((uint8_t)(n >> 8));
-    h.push_back((uint8_t)n);
-  } else {
-    h.push_back(0xdd);
-    for (int i = 3; i >= 0; --i) h.push_back((uint8_t)(n >> (8 * i)));
-  }
-  return h;
-}
-
-struct WireReader {
-  const uint8_t* p;
-  size_t n, i = 0;
-  [[noreturn]] void bad(const char* what) const {
-    fail(HG_ERR_INVALID, std::string("Cannot parse: buffer format error (") + what + ")");
-  }
-  uint64_t be(int k) {
-    if (n - i < (size_t)k) bad("truncated");
-    uint64_t v = 0;
-    for (int j = 0; j < k; ++j) v = (v << 8) | p[i++];
-    return v;
-  }
-  uint8_t byte() { return (uint8_t)be(1); }
-  int64_t integer() {
-    const uint8_t t = byte();
-    if (t < 0x80) return t;
-    if (t >= 0xe0) return (int8_t)t;
-    switch (t) {
-      case 0xcc: return (int64_t)be(1);
-      case 0xcd: return (int64_t)be(2);
-      case 0xce: return (int64_t)be(4);
-      case 0xcf: {
-        const uint64_t v = be(8);
-        if (v > (uint64_t)INT64_MAX) bad("integer");
-        return (int64_t)v;
-      }
-      case 0xd0: return (int8_t)be(1);
-      case 0xd1: return (int16_t)be(2);
-      case 0xd2: return (int32_t)be(4);
-      case 0xd3: return (int64_t)be(8);
-      default: bad("integer");
-    }
-  }
-  uint64_t array() {
-    const uint8_t t = byte();
-    if ((t & 0xf0) == 0x90) return t & 0x0f;
-    if (t == 0xdc) return be(2);
-    if (t == 0xdd) return be(4);
-    bad("array");
-  }
-  // str or bin (msgpack-c's as<std::string_view> takes both)
-  uint64_t bytes() {
-    const uint8_t t = byte();
-    if ((t & 0xe0) == 0xa0) return t & 0x1f;
-    if (t == 0xd9 || t == 0xc4) return be(1);
-    if (t == 0xda || t == 0xc5) return be(2);
-    if (t == 0xdb || t == 0xc6) return be(4);
-    bad("item");
-  }
-};
-
-struct WireIndex {
-  size_t rows = 0, cols = 0;
-  int ndim = 0;
-  std::vector<uint64_t> offs, lens;
-};
-
-// The host walk: header checks of matrix.h:280-292, one offset per item.
-WireIndex wire_walk(const uint8_t* buf, size_t len) {
-  WireReader r{buf, len};
-  WireIndex w;
-  if (r.array() != 4) r.bad("not a 4-element array");
-  const int64_t rows = r.integer(), cols = r.integer(), ndim = r.integer();
-  if (rows < 0 || cols < 0 || ndim < 0 || ndim > 2) r.bad("shape");
-  w.rows = (size_t)rows;
-  w.cols = (size_t)cols;
-  w.ndim = (int)ndim;
-  const uint64_t n = r.array();
-  if ((unsigned __int128)n != (unsigned __int128)(uint64_t)rows * (uint64_t)cols)
-    r.bad("inner array size != rows * cols");
-  if (n > len - r.i) r.bad("truncated");  // every item takes at least one byte
-  w.offs.resize(n);
-  w.lens.resize(n);
-  for (uint64_t k = 0; k < n; ++k) {
-    const uint64_t l = r.bytes();
-    if (len - r.i < l) r.bad("truncated item");
-    w.offs[k] = r.i;
-    w.lens[k] = l;
-    r.i += l;
-  }
-  return w;
-}
 
 void wire_pack(KeyRec& k, Work& w, const uint32_t* dct, size_t rows, size_t cols, int row_major,
                const std::vector<uint8_t>& prefix, uint8_t* host_out, uint8_t* dev_out, size_t cap, size_t* len) {
@@ -1588,24 +1471,37 @@ void wire_pack(KeyRec& k, Work& w, const uint32_t* dct, size_t rows, size_t cols
   }
 }
 
-void wire_unpack(KeyRec& k, Work& w, const uint8_t* buf, const WireIndex& ix, int row_major, uint32_t* dout) {
-  const size_t n = ix.offs.size();
-  if (n == 0) return;
-  // the items span [first offset, end of the last item)
-  const size_t lo = (size_t)ix.offs.front(), hi = (size_t)(ix.offs.back() + ix.lens.back());
-  auto* dbuf = w.io[1].ensure<uint8_t>(hi - lo);
-  auto* doffs = w.io[2].ensure<uint64_t>(n * 8);
-  auto* dlens = w.io[3].ensure<uint64_t>(n * 8);
-  std::vector<uint64_t> rel(n);
-  for (size_t i = 0; i < n; ++i) rel[i] = ix.offs[i] - lo;
-  h2d(dbuf, buf + lo, hi - lo, w);
-  h2d(doffs, rel.data(), n * 8, w);
-  h2d(dlens, ix.lens.data(), n * 8, w);
-  cuda_check(hg::launch_wire_unpack(dbuf, doffs, dlens, ix.rows, ix.cols, row_major, k.S, schema_value(k), dout,
+// Host bytes -> S limbs per item at dout (device).  The buffer's copy to the
+// device is queued first, so the host walk over the item headers runs while
+// it transfers; offsets and lengths go through pinned memory.  Synchronises
+// the stream (also when the walk fails: the copy reads the caller's buffer).
+WireShape wire_load(KeyRec& k, Work& w, const uint8_t* buf, size_t len, int row_major, uint32_t** dout_io,
+                    uint32_t* dout_given, size_t cap_count) {
+  WireReader r{buf, len};
+  const WireShape sh = wire_header(r);
+  if (sh.n > cap_count) {
+    WireShape out = sh;
+    out.n = (size_t)-1;  // tells the caller that the output is too small
+    return out;
+  }
+  if (sh.n == 0) return sh;
+  auto* dbuf = w.io[1].ensure<uint8_t>(len);
+  h2d(dbuf, buf, len, w);
+  auto* pin = w.pin_wire.ensure<uint64_t>(sh.n * 16);
+  try {
+    wire_items(r, sh.n, pin, pin + sh.n, (uint8_t)schema_value(k));
+  } catch (...) {
+    cudaStreamSynchronize(w.stream);
+    throw;
+  }
+  auto* dmeta = w.io[2].ensure<uint64_t>(sh.n * 16);
+  h2d(dmeta, pin, sh.n * 16, w);
+  uint32_t* dout = dout_given ? dout_given : (*dout_io = w.io[0].ensure<uint32_t>(sh.n * ct_bytes(k)));
+  cuda_check(hg::launch_wire_unpack(dbuf, dmeta, dmeta + sh.n, sh.rows, sh.cols, row_major, k.S, schema_value(k), dout,
                                      w.errp(), w.stream),
              "wire read");
-  // rel and the index must outlive the copies: the caller synchronises
   cuda_check(cudaStreamSynchronize(w.stream), "stream sync");
+  return sh;
 }
 
 }  // namespace
@@ -1660,23 +1556,19 @@ int hg_deserialize(hg_ctx* ctx, int key_id, const uint8_t* buf, size_t len, int 
   return guarded(__func__, [&] {
     if (!buf || !rows || !cols || !ndim) fail(HG_ERR_INVALID, "null argument");
     KeyRec* k = get_key(ctx, key_id);
-    const WireIndex ix = wire_walk(buf, len);
-    const size_t n = ix.offs.size();
-    *rows = ix.rows;
-    *cols = ix.cols;
-    *ndim = ix.ndim;
-    if (n > cap_count) fail(HG_ERR_INVALID, "output holds " + std::to_string(cap_count) + " ciphertexts, " +
-                                                std::to_string(n) + " serialized");
-    if (n && !ct_out) fail(HG_ERR_INVALID, "null argument");
-    if (n == 0) return HG_OK;
     set_device(ctx);
     LaneGuard lane(ctx);
     Work& w = *lane.w;
     reset_err(w);
-    const size_t cb = ct_bytes(*k);
-    auto* dout = w.io[0].ensure<uint32_t>(n * cb);
-    wire_unpack(*k, w, buf, ix, row_major, dout);
-    d2h(ct_out, dout, n * cb, w);
+    uint32_t* dout = nullptr;
+    const WireShape sh = wire_load(*k, w, buf, len, row_major, &dout, nullptr, ct_out ? cap_count : 0);
+    *rows = sh.rows;
+    *cols = sh.cols;
+    *ndim = sh.ndim;
+    if (sh.n == (size_t)-1)
+      fail(HG_ERR_INVALID, "output holds " + std::to_string(ct_out ? cap_count : 0) + " ciphertexts, " +
+                               std::to_string(sh.rows * sh.cols) + " serialized");
+    if (sh.n) d2h(ct_out, dout, sh.n * ct_bytes(*k), w);
     finish(w);
     return HG_OK;
   });
@@ -1687,18 +1579,15 @@ int hg_dev_deserialize(hg_ctx* ctx, int key_id, const uint8_t* buf, size_t len, 
   return guarded(__func__, [&] {
     if (!buf || !rows || !cols || !ndim) fail(HG_ERR_INVALID, "null argument");
     KeyRec* k = get_key(ctx, key_id);
-    const WireIndex ix = wire_walk(buf, len);
-    const size_t n = ix.offs.size();
-    *rows = ix.rows;
-    *cols = ix.cols;
-    *ndim = ix.ndim;
-    if (n > cap_count) fail(HG_ERR_INVALID, "output holds " + std::to_string(cap_count) + " ciphertexts, " +
-                                                std::to_string(n) + " serialized");
-    if (n && !ct_out) fail(HG_ERR_INVALID, "null argument");
-    if (n == 0) return HG_OK;
     set_device(ctx);
     Work& w = dev_work(ctx, stream);
-    wire_unpack(*k, w, buf, ix, row_major, ct_out);
+    const WireShape sh = wire_load(*k, w, buf, len, row_major, nullptr, ct_out, ct_out ? cap_count : 0);
+    *rows = sh.rows;
+    *cols = sh.cols;
+    *ndim = sh.ndim;
+    if (sh.n == (size_t)-1)
+      fail(HG_ERR_INVALID, "output holds " + std::to_string(ct_out ? cap_count : 0) + " ciphertexts, " +
+                               std::to_string(sh.rows * sh.cols) + " serialized");
     return HG_OK;
   });
 }

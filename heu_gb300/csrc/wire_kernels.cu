@@ -9,11 +9,12 @@
 // (phe/base/serializable_types.cc:49-69).  The BigInt field c_ is written as
 // a msgpack bin of its little-endian magnitude without leading zero bytes.
 //
-// Packing is byte work bound by HBM: one warp per ciphertext finds its
-// length, a three-kernel exclusive scan places the items, and one warp per
-// ciphertext writes its item with consecutive lanes on consecutive bytes.
-// Unpacking takes the item offsets (found by a host walk over the headers)
-// and turns each item back into S limbs.
+// Packing is byte work bound by HBM: one thread per ciphertext finds its
+// length, a three-kernel exclusive scan places the items, and each warp
+// writes 32 items (a lane per item for the headers, the whole warp on each
+// payload with word stores).  Unpacking takes the item offsets (found by a
+// host walk over the headers) and turns each item back into S limbs the same
+// way round.
 #include <cstdint>
 
 #include "paillier_kernels.cuh"
@@ -29,8 +30,13 @@ constexpr int kScanBlock = 1024;
 
 // Item k of the column-major DenseMatrix order (matrix.h:159-162) is element
 // (k % rows, k / rows); in a row-major array that is (k % rows) * cols + k / rows.
+// A vector or a single row is the same in both orders; otherwise the 32-bit
+// division serves every matrix of fewer than 2^32 elements.
 __device__ __forceinline__ size_t elem_of_item(size_t k, size_t rows, size_t cols, int row_major) {
-  return row_major ? (k % rows) * cols + k / rows : k;
+  if (!row_major || rows == 1 || cols == 1) return k;
+  if ((rows | k) >> 32) return (k % rows) * cols + k / rows;
+  const uint32_t k32 = (uint32_t)k, r32 = (uint32_t)rows, q = k32 / r32;
+  return (size_t)(k32 - q * r32) * cols + q;
 }
 
 __device__ __forceinline__ int bin_header_len(uint32_t b) { return b < 256u ? 2 : (b < 65536u ? 3 : 5); }
@@ -38,25 +44,20 @@ __device__ __forceinline__ int str_header_len(uint64_t l) {
   return l < 32u ? 1 : (l < 256u ? 2 : (l < 65536u ? 3 : 5));
 }
 
-// Per ciphertext: magnitude bytes and the item's total bytes (str header
-// included).
+// Per ciphertext (one thread each): magnitude bytes and the item's total
+// bytes (str header included).  A full-size value has a nonzero top limb, so
+// one 4-byte read usually decides.
 __global__ void k_wire_sizes(const uint32_t* __restrict__ ct, size_t count, size_t rows, size_t cols, int row_major,
                              int S, uint32_t* __restrict__ mag_bytes, uint64_t* __restrict__ item_bytes) {
-  const int lane = threadIdx.x & 31;
-  const size_t i = (size_t)blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= count) return;
   const uint32_t* c = ct + elem_of_item(i, rows, cols, row_major) * (size_t)S;
-  int top = -1;
-  for (int j = lane; j < S; j += 32)
-    if (c[j] != 0u) top = j;
-  top = __reduce_max_sync(0xffffffffu, top + 1) - 1;
-  if (lane == 0) {
-    uint32_t b = 0;
-    if (top >= 0) b = (uint32_t)top * 4u + (uint32_t)((32 - __clz(c[top]) + 7) / 8);
-    const uint64_t inner = 1u + (uint64_t)bin_header_len(b) + b + 8u;  // fixarray(1), bin, schema
-    mag_bytes[i] = b;
-    item_bytes[i] = (uint64_t)str_header_len(inner) + inner;
-  }
+  int top = S - 1;
+  while (top >= 0 && c[top] == 0u) --top;
+  const uint32_t b = top >= 0 ? (uint32_t)top * 4u + (uint32_t)((32 - __clz(c[top]) + 7) / 8) : 0u;
+  const uint64_t inner = 1u + (uint64_t)bin_header_len(b) + b + 8u;  // fixarray(1), bin, schema
+  mag_bytes[i] = b;
+  item_bytes[i] = (uint64_t)str_header_len(inner) + inner;
 }
 
 // Exclusive scan of v within blocks of kScanBlock; block totals to bsum.
@@ -131,73 +132,130 @@ __device__ __forceinline__ void put_be(uint8_t* p, uint64_t v, int n) {
   for (int k = 0; k < n; ++k) p[k] = (uint8_t)(v >> (8 * (n - 1 - k)));
 }
 
-// One warp per ciphertext writes its item at base + its offset.
+// b bytes from the limbs at c (their little-endian magnitude) to the
+// unaligned m, by the whole warp: byte stores up to the first 4-byte boundary
+// of m, then whole words, each funnel-shifted from the two source words it
+// straddles, then the tail bytes.
+__device__ __forceinline__ void copy_payload(uint8_t* m, const uint32_t* c, uint32_t b, int lane) {
+  const uint8_t* src = reinterpret_cast<const uint8_t*>(c);
+  const uint32_t head = min((uint32_t)((4u - ((uint32_t)(uintptr_t)m & 3u)) & 3u), b);
+  if (lane < (int)head) m[lane] = src[lane];
+  const uint32_t nw = (b - head) >> 2, r = head & 3u;
+  uint32_t* dw = reinterpret_cast<uint32_t*>(m + head);
+  for (uint32_t w = lane; w < nw; w += 32) {
+    const uint32_t q = (head + 4u * w) >> 2;  // word of the first byte; with r != 0 the last is q + 1 < S
+    const uint32_t lo = c[q], hi = r ? c[q + 1] : 0u;
+    dw[w] = __funnelshift_r(lo, hi, 8u * r);
+  }
+  const uint32_t done = head + 4u * nw;
+  if (lane < (int)(b - done)) m[done + lane] = src[done + lane];
+}
+
+// Each warp writes 32 consecutive items: every lane the headers and the
+// schema trailer of its own item, then the warp copies the payloads one item
+// after the other.
 __global__ void k_wire_write(const uint32_t* __restrict__ ct, size_t count, size_t rows, size_t cols, int row_major,
                              int S, const uint32_t* __restrict__ mag_bytes, const uint64_t* __restrict__ offs,
                              const uint64_t* __restrict__ bsum, uint64_t schema, uint8_t* __restrict__ out,
                              size_t base) {
   const int lane = threadIdx.x & 31;
-  const size_t i = (size_t)blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
-  if (i >= count) return;
-  const uint32_t b = mag_bytes[i];
-  const uint64_t inner = 1u + (uint64_t)bin_header_len(b) + b + 8u;
-  const int sh = str_header_len(inner), bh = bin_header_len(b);
-  uint8_t* p = out + base + offs[i] + bsum[i / kScanBlock];
-  if (lane == 0) {
+  const size_t first = ((size_t)blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5)) * 32;
+  if (first >= count) return;
+  const size_t i = first + lane;
+  uint32_t b = 0;
+  uint64_t mpos = 0;  // payload position in out
+  uint64_t e = 0;     // element index in ct
+  if (i < count) {
+    b = mag_bytes[i];
+    const uint64_t inner = 1u + (uint64_t)bin_header_len(b) + b + 8u;
+    const int sh = str_header_len(inner), bh = bin_header_len(b);
+    const uint64_t at = base + offs[i] + bsum[i / kScanBlock];
+    uint8_t* p = out + at;
     if (sh == 1) {
       p[0] = (uint8_t)(0xa0u | (uint32_t)inner);
     } else {
       p[0] = sh == 2 ? 0xd9 : (sh == 3 ? 0xda : 0xdb);
       put_be(p + 1, inner, sh - 1);
     }
-    uint8_t* q = p + sh;
-    q[0] = 0x91;  // fixarray(1): MSGPACK_DEFINE(c_)
-    q[1] = bh == 2 ? 0xc4 : (bh == 3 ? 0xc5 : 0xc6);
-    put_be(q + 2, b, bh - 1);
+    p[sh] = 0x91;  // fixarray(1): MSGPACK_DEFINE(c_)
+    p[sh + 1] = bh == 2 ? 0xc4 : (bh == 3 ? 0xc5 : 0xc6);
+    put_be(p + sh + 2, b, bh - 1);
+    mpos = at + (uint64_t)(sh + 1 + bh);
+    uint8_t* tr = out + mpos + b;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) tr[k] = (uint8_t)(schema >> (8 * k));
+    e = elem_of_item(i, rows, cols, row_major);
   }
-  const uint32_t* c = ct + elem_of_item(i, rows, cols, row_major) * (size_t)S;
-  uint8_t* m = p + sh + 1 + bh;
-  for (uint32_t j = lane; j < b; j += 32) m[j] = (uint8_t)(c[j >> 2] >> (8 * (j & 3)));
-  if (lane < 8) m[b + lane] = (uint8_t)(schema >> (8 * lane));
+  const int nitems = (int)min((size_t)32, count - first);
+  for (int t = 0; t < nitems; ++t) {
+    const uint32_t bt = __shfl_sync(0xffffffffu, b, t);
+    const uint64_t mt = __shfl_sync(0xffffffffu, mpos, t);
+    const uint64_t et = __shfl_sync(0xffffffffu, e, t);
+    copy_payload(out + mt, ct + et * (size_t)S, bt, lane);
+  }
 }
 
-// One warp per item: bytes [offs[i], offs[i] + lens[i]) of buf -> S limbs.
+// Each warp reads 32 consecutive items: every lane checks the headers of its
+// own item (bytes [offs[i], offs[i] + lens[i]) of buf), then the warp turns
+// the payloads into S limbs one item after the other.
 __global__ void k_wire_read(const uint8_t* __restrict__ buf, const uint64_t* __restrict__ offs,
                             const uint64_t* __restrict__ lens, size_t count, size_t rows, size_t cols, int row_major,
                             int S, uint64_t schema, uint32_t* __restrict__ out, uint32_t* err) {
   const int lane = threadIdx.x & 31;
-  const size_t i = (size_t)blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
-  if (i >= count) return;
-  const uint8_t* p = buf + offs[i];
-  const uint64_t len = lens[i];
-  uint32_t* o = out + elem_of_item(i, rows, cols, row_major) * (size_t)S;
-  // header checks (every lane reads the same bytes)
-  bool ok = len >= 1u + 2u + 8u && p[0] == 0x91;
-  uint64_t b = 0;
-  int bh = 0;
-  if (ok) {
-    const uint8_t t = p[1];
-    bh = t == 0xc4 ? 2 : (t == 0xc5 ? 3 : (t == 0xc6 ? 5 : 0));
-    ok = bh != 0 && len >= 1u + (uint64_t)bh + 8u;
+  const size_t first = ((size_t)blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5)) * 32;
+  if (first >= count) return;
+  const size_t i = first + lane;
+  bool ok = false;
+  uint64_t b = 0, mpos = 0, e = 0;
+  if (i < count) {
+    const uint8_t* p = buf + offs[i];
+    const uint64_t len = lens[i];
+    ok = len >= 1u + 2u + 8u && p[0] == 0x91;
+    int bh = 0;
     if (ok) {
-      for (int k = 1; k < bh; ++k) b = (b << 8) | p[1 + k];
-      ok = 1u + (uint64_t)bh + b + 8u == len && b <= 4u * (uint64_t)S;
+      const uint8_t t = p[1];
+      bh = t == 0xc4 ? 2 : (t == 0xc5 ? 3 : (t == 0xc6 ? 5 : 0));
+      ok = bh != 0 && len >= 1u + (uint64_t)bh + 8u;
+      if (ok) {
+        for (int k = 1; k < bh; ++k) b = (b << 8) | p[1 + k];
+        ok = 1u + (uint64_t)bh + b + 8u == len && b <= 4u * (uint64_t)S;
+      }
     }
+    if (ok) ok = p[len - 8] == (uint8_t)schema;  // serializable_types.cc:117 reads the low byte
+    if (!ok) atomicOr(err, kErrFormat);
+    mpos = offs[i] + 1u + (uint64_t)bh;
+    e = elem_of_item(i, rows, cols, row_major);
   }
-  if (ok) ok = p[len - 8] == (uint8_t)schema;  // serializable_types.cc:117 reads the low byte
-  if (!ok) {
-    if (lane == 0) atomicOr(err, kErrFormat);
-    for (int j = lane; j < S; j += 32) o[j] = 0u;
-    return;
-  }
-  const uint8_t* m = p + 1 + bh;
-  for (int j = lane; j < S; j += 32) {
-    uint32_t v = 0u;
-    for (int k = 3; k >= 0; --k) {
-      const uint64_t at = 4u * (uint64_t)j + (uint64_t)k;
-      v = (v << 8) | (at < b ? m[at] : 0u);
+  const int nitems = (int)min((size_t)32, count - first);
+  for (int t = 0; t < nitems; ++t) {
+    const bool okt = __shfl_sync(0xffffffffu, ok, t);
+    const uint64_t bt = __shfl_sync(0xffffffffu, b, t);
+    const uint64_t mt = __shfl_sync(0xffffffffu, mpos, t);
+    const uint64_t et = __shfl_sync(0xffffffffu, e, t);
+    uint32_t* o = out + et * (size_t)S;
+    if (!okt) {
+      for (int j = lane; j < S; j += 32) o[j] = 0u;
+      continue;
     }
-    o[j] = v;
+    // limb j = bytes [4j, 4j + 4) of the magnitude (zero past bt): whole limbs
+    // from the aligned words around them, the last partial limb bytewise
+    const uint8_t* m = buf + mt;
+    const uint32_t mis = (uint32_t)(uintptr_t)m & 3u;
+    const uint32_t* aw = reinterpret_cast<const uint32_t*>(m - mis);
+    const uint32_t full = (uint32_t)(bt >> 2);
+    for (int j = lane; j < S; j += 32) {
+      uint32_t v = 0u;
+      if ((uint32_t)j < full) {
+        const uint32_t lo = aw[j], hi = mis ? aw[j + 1] : 0u;  // aw[j + 1] holds bytes < 4j + 4 + mis <= bt + 3
+        v = __funnelshift_r(lo, hi, 8u * mis);
+      } else {
+        for (int k = 3; k >= 0; --k) {
+          const uint64_t at = 4u * (uint64_t)j + (uint64_t)k;
+          v = (v << 8) | (at < bt ? m[at] : 0u);
+        }
+      }
+      o[j] = v;
+    }
   }
 }
 
@@ -215,8 +273,8 @@ cudaError_t launch_wire_size(const uint32_t* ct, size_t rows, size_t cols, int r
   const size_t nb = (count + kScanBlock - 1) / kScanBlock;
   uint64_t* items = scratch;
   uint64_t* bsum = scratch + count;
-  const unsigned g = (unsigned)((count + kWarpsPerBlock - 1) / kWarpsPerBlock);
-  k_wire_sizes<<<g, 32 * kWarpsPerBlock, 0, st>>>(ct, count, rows, cols, row_major, S, mag_bytes, items);
+  const unsigned gs = (unsigned)((count + 255) / 256);
+  k_wire_sizes<<<gs, 256, 0, st>>>(ct, count, rows, cols, row_major, S, mag_bytes, items);
   k_scan_local<<<(unsigned)nb, kScanBlock, 0, st>>>(items, count, bsum);
   k_scan_totals<<<1, kScanBlock, 0, st>>>(bsum, nb);
   count_launches(3);
@@ -230,7 +288,7 @@ cudaError_t launch_wire_write(const uint32_t* ct, size_t rows, size_t cols, int 
                               cudaStream_t st) {
   const size_t count = rows * cols;
   if (count == 0) return cudaSuccess;
-  const unsigned g = (unsigned)((count + kWarpsPerBlock - 1) / kWarpsPerBlock);
+  const unsigned g = (unsigned)((count + 32 * kWarpsPerBlock - 1) / (32 * kWarpsPerBlock));
   k_wire_write<<<g, 32 * kWarpsPerBlock, 0, st>>>(ct, count, rows, cols, row_major, S, mag_bytes, scratch,
                                                    scratch + count, schema, out, base);
   count_launches(1);
@@ -242,7 +300,7 @@ cudaError_t launch_wire_unpack(const uint8_t* buf, const uint64_t* offs, const u
                                cudaStream_t st) {
   const size_t count = rows * cols;
   if (count == 0) return cudaSuccess;
-  const unsigned g = (unsigned)((count + kWarpsPerBlock - 1) / kWarpsPerBlock);
+  const unsigned g = (unsigned)((count + 32 * kWarpsPerBlock - 1) / (32 * kWarpsPerBlock));
   k_wire_read<<<g, 32 * kWarpsPerBlock, 0, st>>>(buf, offs, lens, count, rows, cols, row_major, S, schema, out, err);
   count_launches(1);
   return cudaGetLastError();
