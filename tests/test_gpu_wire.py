@@ -130,6 +130,13 @@ def test_device_forms_match_host_forms(gpu_key):
     capi.check(lib.hg_dev_serialize(h, key.id, ctypes.c_void_p(dct.data_ptr()), 40, 25, 2, 1,
                                     ctypes.c_void_p(dout.data_ptr()), bound.value, ctypes.byref(ln), sp))
     assert ln.value == len(buf) and dout[:ln.value].cpu().numpy().tobytes() == buf
+    # ciphertexts at an address that is 4-byte but not 16-byte aligned
+    shifted = torch.zeros(dct.numel() + 1, dtype=torch.int32, device=dev)
+    shifted[1:].copy_(dct.reshape(-1))
+    dout.zero_()
+    capi.check(lib.hg_dev_serialize(h, key.id, ctypes.c_void_p(shifted.data_ptr() + 4), 40, 25, 2, 1,
+                                    ctypes.c_void_p(dout.data_ptr()), bound.value, ctypes.byref(ln), sp))
+    assert dout[:ln.value].cpu().numpy().tobytes() == buf
     back = torch.empty_like(dct)
     b = np.frombuffer(buf, np.uint8)
     rows, cols, nd = ctypes.c_size_t(), ctypes.c_size_t(), ctypes.c_int()
