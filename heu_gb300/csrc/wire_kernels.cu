@@ -132,32 +132,13 @@ __device__ __forceinline__ void put_be(uint8_t* p, uint64_t v, int n) {
   for (int k = 0; k < n; ++k) p[k] = (uint8_t)(v >> (8 * (n - 1 - k)));
 }
 
-// b bytes from the limbs at c (their little-endian magnitude) to the
-// unaligned m, by the whole warp: byte stores up to the first 4-byte boundary
-// of m, then whole words, each funnel-shifted from the two source words it
-// straddles, then the tail bytes.
-__device__ __forceinline__ void copy_payload(uint8_t* m, const uint32_t* c, uint32_t b, int lane) {
-  const uint8_t* src = reinterpret_cast<const uint8_t*>(c);
-  const uint32_t head = min((uint32_t)((4u - ((uint32_t)(uintptr_t)m & 3u)) & 3u), b);
-  if (lane < (int)head) m[lane] = src[lane];
-  const uint32_t nw = (b - head) >> 2, r = head & 3u;
-  uint32_t* dw = reinterpret_cast<uint32_t*>(m + head);
-  for (uint32_t w = lane; w < nw; w += 32) {
-    const uint32_t q = (head + 4u * w) >> 2;  // word of the first byte; with r != 0 the last is q + 1 < S
-    const uint32_t lo = c[q], hi = r ? c[q + 1] : 0u;
-    dw[w] = __funnelshift_r(lo, hi, 8u * r);
-  }
-  const uint32_t done = head + 4u * nw;
-  if (lane < (int)(b - done)) m[done + lane] = src[done + lane];
-}
-
 // Each warp writes 32 consecutive items: every lane the headers and the
 // schema trailer of its own item, then the warp copies the payloads one item
 // after the other.
 __global__ void k_wire_write(const uint32_t* __restrict__ ct, size_t count, size_t rows, size_t cols, int row_major,
                              int S, const uint32_t* __restrict__ mag_bytes, const uint64_t* __restrict__ offs,
                              const uint64_t* __restrict__ bsum, uint64_t schema, uint8_t* __restrict__ out,
-                             size_t base) {
+                             size_t base, int aligned16) {
   const int lane = threadIdx.x & 31;
   const size_t first = ((size_t)blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5)) * 32;
   if (first >= count) return;
@@ -186,12 +167,64 @@ __global__ void k_wire_write(const uint32_t* __restrict__ ct, size_t count, size
     for (int k = 0; k < 8; ++k) tr[k] = (uint8_t)(schema >> (8 * k));
     e = elem_of_item(i, rows, cols, row_major);
   }
+  // Payloads, four items at a time so that their loads are in flight
+  // together: in each round lane L holds source words w0 .. w0 + 3
+  // (w0 = 128 * round + 4L, one 16-byte load) and writes destination words
+  // w0 .. w0 + 3, word w being source words w and w + 1 shifted by the
+  // payload's misalignment (the next lane's first word, by shuffle; lane 31
+  // loads it).  Head and tail bytes are stored singly.
   const int nitems = (int)min((size_t)32, count - first);
-  for (int t = 0; t < nitems; ++t) {
-    const uint32_t bt = __shfl_sync(0xffffffffu, b, t);
-    const uint64_t mt = __shfl_sync(0xffffffffu, mpos, t);
-    const uint64_t et = __shfl_sync(0xffffffffu, e, t);
-    copy_payload(out + mt, ct + et * (size_t)S, bt, lane);
+  constexpr int kItems = 4;
+  for (int t0 = 0; t0 < nitems; t0 += kItems) {
+    uint32_t bt[kItems];
+    uint8_t* mt[kItems];
+    const uint32_t* ctt[kItems];
+#pragma unroll
+    for (int u = 0; u < kItems; ++u) {
+      const int t = (t0 + u) & 31;
+      bt[u] = __shfl_sync(0xffffffffu, b, t);
+      mt[u] = out + __shfl_sync(0xffffffffu, mpos, t);
+      ctt[u] = ct + __shfl_sync(0xffffffffu, e, t) * (size_t)S;
+      if (t0 + u >= nitems) bt[u] = 0u;  // nothing to copy
+    }
+    for (int w0base = 0; w0base < S; w0base += 128) {
+      const int w0 = w0base + 4 * lane;
+      uint4 v[kItems];
+      uint32_t nx[kItems];
+#pragma unroll
+      for (int u = 0; u < kItems; ++u) {
+        const bool need = bt[u] > 0u && w0 < S && 4u * (uint32_t)w0 < bt[u];
+        if (!need)
+          v[u] = make_uint4(0u, 0u, 0u, 0u);
+        else if (aligned16)
+          v[u] = *reinterpret_cast<const uint4*>(ctt[u] + w0);
+        else
+          v[u] = make_uint4(ctt[u][w0], ctt[u][w0 + 1], ctt[u][w0 + 2], ctt[u][w0 + 3]);
+        nx[u] = (need && lane == 31 && w0 + 4 < S) ? ctt[u][w0 + 4] : 0u;
+      }
+#pragma unroll
+      for (int u = 0; u < kItems; ++u) {
+        const uint32_t down = __shfl_down_sync(0xffffffffu, v[u].x, 1);
+        if (bt[u] == 0u) continue;
+        const uint32_t hi4 = lane == 31 ? nx[u] : down;
+        uint8_t* m = mt[u];
+        const uint32_t head = min((uint32_t)((4u - ((uint32_t)(uintptr_t)m & 3u)) & 3u), bt[u]);
+        const uint32_t nw = (bt[u] - head) >> 2, sh = 8u * (head & 3u);
+        uint32_t* dw = reinterpret_cast<uint32_t*>(m + head);
+        const uint32_t src[5] = {v[u].x, v[u].y, v[u].z, v[u].w, hi4};
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const uint32_t w = (uint32_t)(w0 + j);
+          if (w < nw) dw[w] = __funnelshift_r(src[j], src[j + 1], sh);
+        }
+        if (w0base == 0) {
+          const uint8_t* s8 = reinterpret_cast<const uint8_t*>(ctt[u]);
+          if (lane < (int)head) m[lane] = s8[lane];
+          const uint32_t done = head + 4u * nw;
+          if (lane < (int)(bt[u] - done)) m[done + lane] = s8[done + lane];
+        }
+      }
+    }
   }
 }
 
@@ -289,8 +322,10 @@ cudaError_t launch_wire_write(const uint32_t* ct, size_t rows, size_t cols, int 
   const size_t count = rows * cols;
   if (count == 0) return cudaSuccess;
   const unsigned g = (unsigned)((count + 32 * kWarpsPerBlock - 1) / (32 * kWarpsPerBlock));
+  // 16-byte loads need a 16-byte aligned ct (rows are S * 4 = 256 / 512 / 768 bytes)
+  const int aligned16 = ((uintptr_t)ct & 15u) == 0 && (S * 4) % 16 == 0;
   k_wire_write<<<g, 32 * kWarpsPerBlock, 0, st>>>(ct, count, rows, cols, row_major, S, mag_bytes, scratch,
-                                                   scratch + count, schema, out, base);
+                                                   scratch + count, schema, out, base, aligned16);
   count_launches(1);
   return cudaGetLastError();
 }
