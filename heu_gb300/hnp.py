@@ -16,6 +16,7 @@ Montgomery form with a logical shape, exactly the bytes the C-ABI exchanges.
 """
 
 import os
+import weakref
 
 import numpy as np
 
@@ -106,6 +107,10 @@ class CiphertextArray:
         HEU's msgpack layout, packed on the GPU."""
         return self.kit.key.serialize(self.limbs, self.shape)
 
+    def __reduce__(self):
+        # pickling (pylib PickleSupport): the wire bytes plus the key's n
+        return _unpickle_ciphertexts, (self.serialize(), self.kit.n)
+
     @staticmethod
     def load_from(bytes_buffer, kit):
         """DenseMatrix::LoadFrom (numpy/matrix.h:264-310, pylib ``load_from``).
@@ -172,7 +177,14 @@ def setup(key_size=2048, seed=None, device=0, table_window=0, context=None, sche
     """Key generation (paillier_z/key_generator.cc:26-60 or
     ou/key_generator.cc:26-96, seeded xoshiro256** stream; a random seed when
     none is given) and engine key load -> HeKit.  ``schema`` names the scheme
-    the way heu.phe.setup's SchemaType does (ZPaillier or OU)."""
+    the way heu.phe.setup's SchemaType does (ZPaillier or OU).
+
+    ``setup(public_key)`` with another kit's ``public_key`` dict instead of a
+    key size gives a kit without the secret key, as heu.phe.setup(pk) does
+    for the side that only encrypts and evaluates (pylib/phe_binding
+    bind_phe.cc setup overloads)."""
+    if isinstance(key_size, dict):
+        return _setup_public(key_size, device, table_window, context)
     schema = schema.lower()
     if schema not in SCHEMAS:
         raise ValueError(f"schema must be one of {SCHEMAS}")
@@ -186,7 +198,38 @@ def setup(key_size=2048, seed=None, device=0, table_window=0, context=None, sche
     else:
         k = engine.keygen(key_size, seed)
         key = ctx.load_key(key_size, k["n"], k["h_s"], k["p"], k["q"], table_window=table_window)
-    return HeKit(ctx, key, k, schema)
+    return HeKit(ctx, key, dict(k, key_bits=key_size), schema)
+
+
+def _setup_public(pk, device, table_window, context):
+    schema = "ou" if "G" in pk else "zpaillier"
+    n = int(pk["n"])
+    # a k-bit key has an n of k bits (ZPaillier) or a few bits more (OU, ou/key_generator.cc:30-52)
+    bits = int(pk.get("key_bits") or (n.bit_length() // 1024) * 1024)
+    ctx = context or engine.Context(device)
+    if schema == "ou":
+        key = ctx.load_ou_key(bits, n, int(pk["G"]), int(pk["H"]), int(pk["max_pt_bits"]), table_window=table_window)
+    else:
+        key = ctx.load_key(bits, n, int(pk["h_s"]), table_window=table_window)
+    return HeKit(ctx, key, dict(pk, key_bits=bits), schema)
+
+
+# Live kits by key, so that unpickled ciphertext arrays find an engine key
+# for their n (the pickle holds the wire bytes, not a device handle).
+_KITS = weakref.WeakValueDictionary()
+
+
+def _kit_for(n):
+    kits = [k for k in list(_KITS.values()) if k.n == n]
+    with_secret = [k for k in kits if k.secret_key is not None]
+    return (with_secret or kits or [None])[-1]
+
+
+def _unpickle_ciphertexts(buf, n):
+    kit = _kit_for(n)
+    if kit is None:
+        raise ValueError("no HeKit for this public key in this process: call hnp.setup(public_key) first")
+    return CiphertextArray.load_from(buf, kit)
 
 
 class HeKit:
@@ -202,15 +245,17 @@ class HeKit:
         self.schema = schema
         self.n = key_ints["n"]
         if schema == "ou":
-            self.public_key = {k: key_ints[k] for k in ("n", "G", "H")}
-            self.secret_key = {k: key_ints[k] for k in ("p", "q", "t", "gp_inv")}
+            pub, sec = ("n", "G", "H", "max_pt_bits", "key_bits"), ("p", "q", "t", "gp_inv")
             self.max_plaintext = 1 << key_ints["max_pt_bits"]
             self.random_bits = engine.ou_random_bits(self.n.bit_length())
         else:
-            self.public_key = {"n": key_ints["n"], "h_s": key_ints["h_s"]}
-            self.secret_key = {"p": key_ints["p"], "q": key_ints["q"]}
+            pub, sec = ("n", "h_s", "key_bits"), ("p", "q")
             self.max_plaintext = self.n // 2
             self.random_bits = None
+        self.public_key = {k: key_ints[k] for k in pub if k in key_ints}
+        has_secret = all(key_ints.get(k) is not None for k in sec)
+        self.secret_key = {k: key_ints[k] for k in sec} if has_secret else None
+        _KITS[id(self)] = self
 
     def array(self, values):
         return PlaintextArray(values)
@@ -219,6 +264,8 @@ class HeKit:
         return Encryptor(self, r_source)
 
     def decryptor(self):
+        if self.secret_key is None:
+            raise ValueError("this HeKit was set up from a public key and cannot decrypt")
         return Decryptor(self)
 
     def evaluator(self):

@@ -170,3 +170,31 @@ def test_full_size_round_trip(gpu_key):
     prefix = b"\x94" + wire._uint(n) + wire._uint(1) + wire._uint(1) + wire._array_header(n)
     assert len(buf) == len(prefix) + int(items.sum()) and buf.startswith(prefix)
     assert wire.parse_item(buf[-int(inner[-1]):]) == (hg.limbs_to_ints(ct[-1:])[0], 4)
+
+
+def test_pickling_and_public_key_kits(gpu_ctx):
+    """heu/pylib/phe_test.py:256-270 flow: a client pickles ciphertexts, a
+    server set up from the client's public key evaluates on them without the
+    secret key, the client unpickles the result and decrypts."""
+    import pickle
+
+    client = hnp.setup(1024, seed=6, context=gpu_ctx, table_window=8)
+    server = hnp.setup(dict(client.public_key), context=gpu_ctx, table_window=8)
+    assert server.secret_key is None and server.n == client.n
+    with pytest.raises(ValueError):
+        server.decryptor()
+    a = np.array([[1, -2], [3, 4]])
+    x = client.encryptor().encrypt(client.array(a))
+    y = pickle.loads(pickle.dumps(x))
+    assert y.kit is client and np.array_equal(y.limbs, x.limbs)
+    on_server = hnp.CiphertextArray.load_from(x.serialize(), server)
+    ev = server.evaluator()
+    z = ev.mul(ev.add(on_server, server.encryptor().encrypt(server.array([10, 20]))), server.array([2, 3]))
+    back = pickle.loads(pickle.dumps(z))
+    assert back.kit is client
+    assert np.array_equal(client.decryptor().decrypt(back).to_numpy(), (a + [10, 20]) * [2, 3])
+    ou_client = hnp.setup(1024, seed=2, context=gpu_ctx, table_window=8, schema="ou")
+    ou_server = hnp.setup(dict(ou_client.public_key), context=gpu_ctx, table_window=8)
+    assert ou_server.schema == "ou" and ou_server.secret_key is None
+    c = ou_server.encryptor().encrypt(ou_server.array([5, -6]))
+    assert ou_client.decryptor().decrypt(pickle.loads(pickle.dumps(c))).to_numpy().tolist() == [5, -6]
