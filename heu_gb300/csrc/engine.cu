@@ -1321,10 +1321,32 @@ int hg_decrypt_bn(hg_ctx* ctx, int key_id, const uint32_t* ct, uint32_t* m_mag, 
   });
 }
 
+// The device address of page-locked host memory (cudaHostAlloc /
+// cudaHostRegister, mapped into the device's address space), else nullptr.
+void* mapped_host_ptr(const void* p) {
+  cudaPointerAttributes pa{};
+  if (cudaPointerGetAttributes(&pa, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return pa.type == cudaMemoryTypeHost ? pa.devicePointer : nullptr;
+}
+
 int hg_add(hg_ctx* ctx, int key_id, const uint32_t* a, const uint32_t* b, uint32_t* out, size_t count) {
   return guarded(__func__, [&] {
     if (!a || !b || !out) fail(HG_ERR_INVALID, "null argument");
     HG_HOST_PROLOGUE
+    // Add is one multiplication per ciphertext, so copies would dominate it:
+    // when all three buffers are page-locked host memory the kernel reads and
+    // writes them in place over the host link instead.
+    const auto* ma = static_cast<const uint32_t*>(mapped_host_ptr(a));
+    const auto* mb = static_cast<const uint32_t*>(mapped_host_ptr(b));
+    auto* mo = static_cast<uint32_t*>(mapped_host_ptr(out));
+    if (ma && mb && mo) {
+      cuda_check(hg::launch_add(k->S, k->kc, ma, mb, mo, count, w.errp(), w.stream), "add launch");
+      finish(w);
+      return HG_OK;
+    }
     run_chunked(ctx, w, count, [&](Work& v, size_t off, size_t cnt) {
       auto* da = v.io[0].ensure<uint32_t>(cnt * cb);
       auto* db = v.io[1].ensure<uint32_t>(cnt * cb);

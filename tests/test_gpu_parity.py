@@ -536,3 +536,33 @@ def test_chunked_host_calls_from_threads(gpu_key):
     for t in ths:
         t.join()
     assert not errors, errors
+
+
+def test_add_on_page_locked_host_buffers(gpu_key):
+    """hg_add with all three buffers page-locked reads and writes them in
+    place from the kernel; results equal the copy path's (pageable buffers),
+    also with out aliasing a."""
+    import ctypes
+
+    torch = pytest.importorskip("torch")
+    key, pk, sk = gpu_key(2048, 0)
+    n = 3000
+    rng = np.random.default_rng(41)
+    m = rng.integers(-(2 ** 40), 2 ** 40, size=n, dtype=np.int64)
+    r = rng.integers(0, 2 ** 32, size=(n, key.r_limbs), dtype=np.uint64).astype(np.uint32)
+    a = key.encrypt(m, r)
+    b = key.encrypt(m[::-1].copy(), r)
+    want = key.add(a, b)  # pageable numpy buffers: the copy path
+    pa = torch.from_numpy(a.view(np.int32)).pin_memory()
+    pb = torch.from_numpy(b.view(np.int32)).pin_memory()
+    po = torch.empty_like(pa).pin_memory()
+    P = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+    capi.check(key.lib.hg_add(key.ctx.handle, key.id, P(pa), P(pb), P(po), n))
+    assert np.array_equal(po.numpy().view(np.uint32), want)
+    capi.check(key.lib.hg_add(key.ctx.handle, key.id, P(pa), P(pb), P(pa), n))
+    assert np.array_equal(pa.numpy().view(np.uint32), want)
+    bad = pb.clone().pin_memory()
+    bad[7] = -1  # >= n^2
+    with pytest.raises(hg.HgError) as ei:
+        capi.check(key.lib.hg_add(key.ctx.handle, key.id, P(po), P(bad), P(po), n))
+    assert ei.value.code == capi.HG_ERR_CT_RANGE
