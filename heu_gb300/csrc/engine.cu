@@ -363,17 +363,21 @@ constexpr size_t kPipeMinChunk = (size_t)1 << 16;
 constexpr size_t kPipeMaxChunks = 8;
 
 // prepare(w) runs on each lane before its first chunk, check(w) on each lane
-// after both drained (the error words are raised first).
+// after both drained (the error words are raised first).  max_chunks bounds
+// the chunks: an op with a per-chunk sequential tail (the batch inverse's
+// tree and host inversion, which wait for the other lane's persistent kernel
+// to leave the SMs) is best split in two.
 template <class F, class Prep, class Check>
-void run_chunked(hg_ctx* ctx, Work& w0, size_t count, F&& chunk, Prep&& prepare, Check&& check) {
-  if (count >= 2 * kPipeMinChunk) {
+void run_chunked(hg_ctx* ctx, Work& w0, size_t count, F&& chunk, Prep&& prepare, Check&& check,
+                 size_t max_chunks = kPipeMaxChunks) {
+  if (count >= 2 * kPipeMinChunk && max_chunks >= 2) {
     ExtraLane extra(ctx);
     if (extra.w) {
       Work& w1 = *extra.w;
       reset_err(w1);
       prepare(w0);
       prepare(w1);
-      const size_t nch = std::min(kPipeMaxChunks, count / kPipeMinChunk);
+      const size_t nch = std::min(max_chunks, count / kPipeMinChunk);
       const size_t per = (count + nch - 1) / nch;
       Work* lanes[2] = {&w0, &w1};
       size_t c = 0;
@@ -1443,7 +1447,7 @@ int hg_mul(hg_ctx* ctx, int key_id, const uint32_t* a, const int64_t* kk, uint32
       h2d(dk, kk + off, cnt * 8, v);
       core_mul(*k, v, da, dk, kk + off, dout, cnt, false);
       d2h((uint8_t*)out + off * cb, dout, cnt * cb, v);
-    }, [](Work& v) { v.task.status = 0; }, [](Work& v) { raise_task_status(v.task); });
+    }, [](Work& v) { v.task.status = 0; }, [](Work& v) { raise_task_status(v.task); }, 2);
     return HG_OK;
   });
 }
