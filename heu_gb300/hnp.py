@@ -10,8 +10,9 @@ batch_select_sum, feature_wise_bucket_sum and batch_feature_wise_bucket_sum.
 Two schemes: ZPaillier (the default) and OU (``setup(..., schema="ou")``,
 heu/library/algorithms/ou), both on the same kernels.  Plaintexts are
 integers (int64 NumPy arrays, or Python ints up to the scheme's plaintext
-bound in an object array); ``BatchEncoder`` packs two int64 values per
-plaintext.  Ciphertexts are kept as a (size, S) uint32 limb array in
+bound in an object array), or floats / scaled integers through
+``FloatEncoder`` / ``IntegerEncoder``; ``BatchEncoder`` packs two int64
+values per plaintext.  Ciphertexts are kept as a (size, S) uint32 limb array in
 Montgomery form with a logical shape, exactly the bytes the C-ABI exchanges.
 """
 
@@ -58,8 +59,10 @@ class PlaintextArray:
     def __getitem__(self, item):
         return PlaintextArray(self.values[item])
 
-    def to_numpy(self):
-        return self.values.copy()
+    def to_numpy(self, encoder=None):
+        """The values, or the values decoded by ``encoder`` (heu.numpy
+        PMatrix.to_numpy(encoder), bind_numpy.cc:75-92)."""
+        return encoder.decode(self.values) if encoder is not None else self.values.copy()
 
     def __str__(self):
         return str(self.values)
@@ -118,6 +121,57 @@ class CiphertextArray:
         engine of ``kit``'s key, so the kit is an argument."""
         limbs, shape = kit.key.deserialize(bytes_buffer)
         return CiphertextArray(kit, limbs, shape)
+
+
+class IntegerEncoder:
+    """PlainEncoder (phe/encoding/plain_encoder.h:46-74) as pylib's
+    IntegerEncoder: encode = value * scale (integers exactly, floats as the
+    double product truncated toward zero, as a BigInt built from a double);
+    decode = value / scale with C++ integer division (toward zero)."""
+
+    def __init__(self, scale=1):
+        self.scale = int(scale)
+        if self.scale <= 0:
+            raise ValueError("scale must be positive")
+
+    def encode(self, values):
+        a = np.asarray(values)
+        s = self.scale
+        if a.dtype.kind == "f":
+            r = np.trunc(a.astype(np.float64) * float(s))
+            if r.size == 0 or np.abs(r).max() < 2.0 ** 63:
+                return r.astype(np.int64)
+            out = np.empty(r.size, dtype=object)
+            out[:] = [int(v) for v in r.reshape(-1)]
+            return out.reshape(r.shape)
+        v = _as_values(a)
+        if v.dtype != object and (v.size == 0 or int(np.abs(v).max()) <= _I64_MAX // s):
+            return v * s
+        return _as_values(np.array([int(x) * s for x in v.reshape(-1)], dtype=object).reshape(v.shape))
+
+    def decode(self, values):
+        v = _as_values(values)
+        s = self.scale
+        if v.dtype != object:
+            q = np.abs(v) // s
+            return np.where(v < 0, -q, q)
+        out = np.empty(v.size, dtype=object)
+        out[:] = [(-1 if x < 0 else 1) * (abs(int(x)) // s) for x in v.reshape(-1)]
+        return out.reshape(v.shape)
+
+
+class FloatEncoder(IntegerEncoder):
+    """pylib FloatEncoder over the same PlainEncoder (default scale 10^6):
+    decode = the value as a double / scale."""
+
+    def __init__(self, scale=10 ** 6):
+        super().__init__(scale)
+
+    def decode(self, values):
+        v = _as_values(values)
+        if v.dtype != object:
+            return v.astype(np.float64) / self.scale
+        return np.array([float(int(x)) / self.scale for x in v.reshape(-1)], dtype=np.float64).reshape(v.shape)
 
 
 class BatchEncoder:
@@ -257,8 +311,16 @@ class HeKit:
         self.secret_key = {k: key_ints[k] for k in sec} if has_secret else None
         _KITS[id(self)] = self
 
-    def array(self, values):
-        return PlaintextArray(values)
+    def array(self, values, encoder=None):
+        """hnp.array(ndarray, encoder): values encoded by ``encoder`` when one
+        is given (integers as they are otherwise)."""
+        return PlaintextArray(encoder.encode(values) if encoder is not None else values)
+
+    def integer_encoder(self, scale=1):
+        return IntegerEncoder(scale)
+
+    def float_encoder(self, scale=10 ** 6):
+        return FloatEncoder(scale)
 
     def encryptor(self, r_source=None):
         return Encryptor(self, r_source)

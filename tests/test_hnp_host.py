@@ -75,3 +75,24 @@ def test_ou_randomness_has_exact_bits():
         r = hnp.Encryptor(kit)._r(64)
         vals = [sum(int(w) << (32 * i) for i, w in enumerate(row)) for row in r]
         assert all(v.bit_length() == bits for v in vals)
+
+
+def test_plain_encoders_follow_plain_encoder_h():
+    """plain_encoder.h:46-74: Encode = value * scale (a double product
+    truncated toward zero), Decode = value / scale (C++ integer division for
+    IntegerEncoder, a double for FloatEncoder)."""
+    fe = hnp.FloatEncoder()
+    enc = fe.encode(np.array([1.5, -1.5, 0.1234567, -2.0000009, 0.0]))
+    assert enc.dtype == np.int64 and enc.tolist() == [1500000, -1500000, 123456, -2000000, 0]
+    assert np.allclose(fe.decode(enc), [1.5, -1.5, 0.123456, -2.0, 0.0])
+    ie = hnp.IntegerEncoder(scale=100)
+    assert ie.encode([3, -7]).tolist() == [300, -700]
+    assert ie.encode(np.array([2.99, -2.99])).tolist() == [299, -299]
+    assert ie.decode(np.array([299, -299, 100, -100])).tolist() == [2, -2, 1, -1]
+    big = ie.encode([2 ** 62, -(2 ** 62)])
+    assert big.dtype == object and big.tolist() == [2 ** 62 * 100, -(2 ** 62) * 100]
+    assert ie.decode(big).tolist() == [2 ** 62, -(2 ** 62)]
+    a = hnp.PlaintextArray(fe.encode([[0.5, -0.25]]))
+    assert a.to_numpy(fe).tolist() == [[0.5, -0.25]]
+    with pytest.raises(ValueError):
+        hnp.IntegerEncoder(0)
