@@ -184,3 +184,20 @@ def test_ou_schema_through_the_numpy_layer(gpu_ctx, bits, seed):
     assert dec.decrypt(enc.encrypt(kit.array([big, -big]))).to_numpy().tolist() == [big, -big]
     with pytest.raises(ValueError, match="out of range"):
         enc.encrypt(kit.array([big + 1]))
+
+
+def test_float_and_integer_encoders_through_the_engine(kit):
+    """hnp.array(ndarray, FloatEncoder) -> Encrypt -> Add / Mul by an
+    integer -> Decrypt -> to_numpy(FloatEncoder), as heu.numpy's float
+    workflow (pylib numpy_test.py uses FloatEncoder the same way)."""
+    fe = kit.float_encoder()
+    x = np.array([[1.25, -2.5], [0.000001, 3.75]])
+    y = np.array([[0.5, 0.5], [-1.0, 2.0]])
+    enc, dec, ev = kit.encryptor(), kit.decryptor(), kit.evaluator()
+    cx = enc.encrypt(kit.array(x, fe))
+    s = ev.add(cx, kit.array(y, fe))
+    got = dec.decrypt(ev.mul(s, kit.array([3, -2]))).to_numpy(fe)
+    assert np.allclose(got, (x + y) * [3, -2])
+    ie = kit.integer_encoder(10)
+    ci = enc.encrypt(kit.array([7, -8], ie))
+    assert dec.decrypt(ci).to_numpy(ie).tolist() == [7, -8]
