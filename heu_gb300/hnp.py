@@ -96,6 +96,26 @@ class CiphertextArray:
         idx = np.asarray(idx)
         return CiphertextArray(self.kit, self.limbs[idx.reshape(-1)], idx.shape)
 
+    def __setitem__(self, item, value):
+        """x[item] = ciphertexts (a CiphertextArray of the same key), with
+        NumPy's indexing and broadcasting (bind_numpy.cc __setitem__)."""
+        if not isinstance(value, CiphertextArray):
+            raise TypeError("only ciphertexts can be assigned into a CiphertextArray")
+        sel = np.asarray(np.arange(self.size).reshape(self.shape)[item])
+        src = np.broadcast_to(np.arange(value.size).reshape(value.shape), sel.shape)
+        self.limbs[sel.reshape(-1)] = value.limbs[src.reshape(-1)]
+
+    def transpose(self):
+        """DenseMatrix::Transpose (numpy/matrix.h:203-206): 2-d arrays only."""
+        if self.ndim != 2:
+            raise ValueError(f"you cannot transpose a {self.ndim}d-tensor")
+        idx = np.arange(self.size).reshape(self.shape).T.reshape(-1)
+        return CiphertextArray(self.kit, self.limbs[idx], self.shape[::-1])
+
+    @property
+    def T(self):
+        return self.transpose()
+
     def grid(self):
         """limbs as (*shape, S)"""
         return self.limbs.reshape(self.shape + (self.kit.key.ct_limbs,))

@@ -96,3 +96,26 @@ def test_plain_encoders_follow_plain_encoder_h():
     assert a.to_numpy(fe).tolist() == [[0.5, -0.25]]
     with pytest.raises(ValueError):
         hnp.IntegerEncoder(0)
+
+
+class _FakeKit:
+    class key:  # noqa: N801
+        ct_limbs = 2
+        key_bits = 64
+
+
+def test_ciphertext_array_transpose_and_setitem_move_limbs():
+    limbs = np.arange(12, dtype=np.uint32).reshape(6, 2)  # six "ciphertexts" of two limbs
+    x = hnp.CiphertextArray(_FakeKit, limbs, (2, 3))
+    t = x.transpose()
+    assert t.shape == (3, 2)
+    assert t.limbs[:, 0].tolist() == [0, 6, 2, 8, 4, 10]  # element (i, j) of t is (j, i) of x
+    with pytest.raises(ValueError):
+        hnp.CiphertextArray(_FakeKit, limbs, (6,)).transpose()
+    y = hnp.CiphertextArray(_FakeKit, np.full((2, 2), 99, np.uint32), (2,))
+    x[1, 1:] = y
+    assert x.limbs[:, 0].tolist() == [0, 2, 4, 6, 99, 99]
+    x[0] = hnp.CiphertextArray(_FakeKit, np.full((1, 2), 7, np.uint32), ())  # broadcast one ciphertext
+    assert x.limbs[:3, 0].tolist() == [7, 7, 7]
+    with pytest.raises(TypeError):
+        x[0, 0] = 5
