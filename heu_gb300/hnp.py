@@ -26,6 +26,10 @@ from heu_gb300 import engine
 _I64_MIN, _I64_MAX = -(2 ** 63), 2 ** 63 - 1
 
 
+def _hex(v):
+    return ("-" if v < 0 else "") + format(abs(v), "X")
+
+
 def _as_values(values):
     a = np.asarray(values, dtype=object) if not isinstance(values, np.ndarray) else values
     if a.dtype != object:
@@ -380,17 +384,37 @@ class Encryptor:
         return r
 
     def encrypt(self, pt):
+        return self._encrypt(pt)[0]
+
+    def _encrypt(self, pt):
         pt = pt if isinstance(pt, PlaintextArray) else PlaintextArray(pt)
         key = self.kit.key
         flat = pt.values.reshape(-1)
+        r = self._r(flat.size)
         if flat.dtype == object:
             bound = self.kit.max_plaintext
             if any(abs(int(v)) > bound for v in flat):
                 raise ValueError("message number out of range")
-            limbs = key.encrypt_bn([int(v) for v in flat], self._r(flat.size))
+            limbs = key.encrypt_bn([int(v) for v in flat], r)
         else:
-            limbs = key.encrypt(flat, self._r(flat.size))
-        return CiphertextArray(self.kit, limbs, pt.shape)
+            limbs = key.encrypt(flat, r)
+        return CiphertextArray(self.kit, limbs, pt.shape), pt, r
+
+    def encrypt_with_audit(self, pt):
+        """EncryptWithAudit (numpy/encryptor.cc:69-104 over
+        paillier_zahlen/encryptor.cc:35-65, ou/encryptor.cc:106-136): the
+        ciphertexts and, per element, "p:<m>,rn:<h_s^r>,c:<c>" (ZPaillier) or
+        "p:<m>,hr:<H^r>,c:<c>" (OU), upper-case hex of the Montgomery-form
+        values as BigInt::ToHexString writes them."""
+        ct, pt, r = self._encrypt(pt)
+        rn = self.kit.key.encrypt_zero(r)
+        tag = "hr" if self.kit.schema == "ou" else "rn"
+        ints = engine.limbs_to_ints
+        audit = [f"p:{_hex(int(m))},{tag}:{_hex(a)},c:{_hex(c)}"
+                 for m, a, c in zip(pt.values.reshape(-1), ints(rn), ints(ct.limbs))]
+        out = np.empty(len(audit), dtype=object)
+        out[:] = audit
+        return ct, out.reshape(pt.shape)
 
     def encrypt_zero(self, shape=()):
         count = int(np.prod(shape, dtype=np.int64))

@@ -201,3 +201,17 @@ def test_float_and_integer_encoders_through_the_engine(kit):
     ie = kit.integer_encoder(10)
     ci = enc.encrypt(kit.array([7, -8], ie))
     assert dec.decrypt(ci).to_numpy(ie).tolist() == [7, -8]
+
+
+def test_encrypt_with_audit_matches_oracle(kit):
+    """EncryptWithAudit: "p:<m>,rn:<h_s^r>,c:<c>" with the Montgomery-form
+    values the oracle gives for the same r (paillier_zahlen/encryptor.cc:50-54)."""
+    pk, sk = oracle_key(1024, 1)
+    src, rs = _stream(17)
+    ct, audit = kit.encryptor(src).encrypt_with_audit(kit.array([[7, -9]]))
+    assert ct.shape == (1, 2) and audit.shape == (1, 2)
+    for j, m in enumerate((7, -9)):
+        rn = pz.to_mont(pk, pz.encrypt_zero(pk, rs[j]))
+        c = pz.to_mont(pk, pz.encrypt(pk, m, rs[j]))
+        sign = "-" if m < 0 else ""
+        assert audit[0, j] == f"p:{sign}{abs(m):X},rn:{rn:X},c:{c:X}"

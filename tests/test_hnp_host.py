@@ -119,3 +119,40 @@ def test_ciphertext_array_transpose_and_setitem_move_limbs():
     assert x.limbs[:3, 0].tolist() == [7, 7, 7]
     with pytest.raises(TypeError):
         x[0, 0] = 5
+
+
+def test_encrypt_with_audit_strings():
+    """Audit strings as paillier_zahlen/encryptor.cc:50-54 and
+    ou/encryptor.cc:110-114 write them (upper-case hex of m, of the
+    randomness term and of c), one per element, in the plaintext's shape;
+    the engine key is a stand-in that records its inputs."""
+
+    class _Key:
+        ct_limbs, r_limbs = 2, 1
+
+        def encrypt(self, m, r):
+            out = np.zeros((len(m), 2), np.uint32)
+            out[:, 0] = (np.asarray(m) + 1000).astype(np.uint32)
+            out[:, 1] = np.asarray(r).reshape(-1)
+            return out
+
+        def encrypt_zero(self, r):
+            out = np.zeros((r.shape[0], 2), np.uint32)
+            out[:, 0] = r[:, 0] * 2
+            return out
+
+    class _Kit:
+        key = _Key()
+        random_bits = None
+        max_plaintext = 2 ** 40
+
+    for schema, tag in (("zpaillier", "rn"), ("ou", "hr")):
+        kit = _Kit()
+        kit.schema = schema
+        enc = hnp.Encryptor(kit, r_source=lambda n: np.arange(1, n + 1, dtype=np.uint32).reshape(n, 1))
+        ct, audit = enc.encrypt_with_audit(hnp.PlaintextArray([[5, -3]]))
+        assert ct.shape == (1, 2) and audit.shape == (1, 2)
+        c0 = 1005 + (1 << 32)  # limbs (m + 1000, r) as one integer
+        c1 = 997 + (2 << 32)
+        assert audit[0, 0] == f"p:5,{tag}:2,c:{c0:X}"
+        assert audit[0, 1] == f"p:-3,{tag}:4,c:{c1:X}"
