@@ -156,3 +156,33 @@ def test_encrypt_with_audit_strings():
         c1 = 997 + (2 << 32)
         assert audit[0, 0] == f"p:5,{tag}:2,c:{c0:X}"
         assert audit[0, 1] == f"p:-3,{tag}:4,c:{c1:X}"
+
+
+def test_setup_from_public_key_picks_scheme_and_key_size():
+    """hnp.setup(public_key): the scheme from the key's fields, the key size
+    from key_bits or from n (a k-bit ZPaillier n has k bits, an OU n a few
+    more), no secret part; the context is a stand-in that records the load."""
+    calls = []
+
+    class _Key:
+        ct_limbs, r_limbs, pt_limbs = 32, 16, 16
+
+    class _Ctx:
+        def load_key(self, bits, n, h_s, p=None, q=None, table_window=0):
+            calls.append(("z", bits, p, q))
+            return _Key()
+
+        def load_ou_key(self, bits, n, G, H, max_pt_bits, p=None, q=None, t=None, gp_inv=None, table_window=0):
+            calls.append(("ou", bits, max_pt_bits, p))
+            return _Key()
+
+    n2048 = (1 << 2047) + 12345
+    kit = hnp.setup({"n": n2048, "h_s": 7}, context=_Ctx())
+    assert calls[-1] == ("z", 2048, None, None) and kit.schema == "zpaillier" and kit.secret_key is None
+    with pytest.raises(ValueError, match="public key"):
+        kit.decryptor()
+    ou_n = (1 << 2050) + 99  # 2051 bits for a 2048-bit OU key
+    kit = hnp.setup({"n": ou_n, "G": 3, "H": 5, "max_pt_bits": 680}, context=_Ctx())
+    assert calls[-1] == ("ou", 2048, 680, None) and kit.schema == "ou" and kit.max_plaintext == 1 << 680
+    kit = hnp.setup({"n": n2048, "h_s": 7, "key_bits": 2048}, context=_Ctx())
+    assert calls[-1][1] == 2048 and kit.public_key["key_bits"] == 2048
