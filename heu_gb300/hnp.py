@@ -21,7 +21,7 @@ import weakref
 
 import numpy as np
 
-from heu_gb300 import engine
+from heu_gb300 import engine, keywire
 
 _I64_MIN, _I64_MAX = -(2 ** 63), 2 ** 63 - 1
 
@@ -251,18 +251,20 @@ class BatchEncoder:
 SCHEMAS = ("zpaillier", "ou")
 
 
-def setup(key_size=2048, seed=None, device=0, table_window=0, context=None, schema="zpaillier"):
+def setup(key_size=2048, seed=None, device=0, table_window=0, context=None, schema="zpaillier", secret_key=None):
     """Key generation (paillier_z/key_generator.cc:26-60 or
     ou/key_generator.cc:26-96, seeded xoshiro256** stream; a random seed when
     none is given) and engine key load -> HeKit.  ``schema`` names the scheme
     the way heu.phe.setup's SchemaType does (ZPaillier or OU).
 
-    ``setup(public_key)`` with another kit's ``public_key`` dict instead of a
-    key size gives a kit without the secret key, as heu.phe.setup(pk) does
-    for the side that only encrypts and evaluates (pylib/phe_binding
-    bind_phe.cc setup overloads)."""
-    if isinstance(key_size, dict):
-        return _setup_public(key_size, device, table_window, context)
+    ``setup(public_key)`` with another kit's ``public_key`` dict (or its
+    ``public_key_bytes()``, HEU's key wire format) instead of a key size gives
+    a kit without the secret key, as heu.phe.setup(pk) does for the side that
+    only encrypts and evaluates; ``secret_key=`` (a ``secret_key`` dict or
+    ``secret_key_bytes()``) makes it a full kit, as setup(pk, sk) does
+    (pylib/phe_binding bind_phe.cc setup overloads)."""
+    if isinstance(key_size, (dict, bytes, bytearray)):
+        return _setup_public(key_size, device, table_window, context, secret_key)
     schema = schema.lower()
     if schema not in SCHEMAS:
         raise ValueError(f"schema must be one of {SCHEMAS}")
@@ -279,17 +281,25 @@ def setup(key_size=2048, seed=None, device=0, table_window=0, context=None, sche
     return HeKit(ctx, key, dict(k, key_bits=key_size), schema)
 
 
-def _setup_public(pk, device, table_window, context):
+def _setup_public(pk, device, table_window, context, sk=None):
+    if isinstance(pk, (bytes, bytearray)):
+        _, pk = keywire.deserialize_public_key(pk)
+    if isinstance(sk, (bytes, bytearray)):
+        _, sk = keywire.deserialize_secret_key(sk)
     schema = "ou" if "G" in pk else "zpaillier"
     n = int(pk["n"])
+    if sk is not None and int(sk.get("n", n)) != n:
+        raise ValueError("pk and sk are not paired")
     # a k-bit key has an n of k bits (ZPaillier) or a few bits more (OU, ou/key_generator.cc:30-52)
     bits = int(pk.get("key_bits") or (n.bit_length() // 1024) * 1024)
     ctx = context or engine.Context(device)
+    sec = {k: int(v) for k, v in (sk or {}).items() if k != "n"}
     if schema == "ou":
-        key = ctx.load_ou_key(bits, n, int(pk["G"]), int(pk["H"]), int(pk["max_pt_bits"]), table_window=table_window)
+        key = ctx.load_ou_key(bits, n, int(pk["G"]), int(pk["H"]), int(pk["max_pt_bits"]), sec.get("p"),
+                              sec.get("q"), sec.get("t"), sec.get("gp_inv"), table_window=table_window)
     else:
-        key = ctx.load_key(bits, n, int(pk["h_s"]), table_window=table_window)
-    return HeKit(ctx, key, dict(pk, key_bits=bits), schema)
+        key = ctx.load_key(bits, n, int(pk["h_s"]), sec.get("p"), sec.get("q"), table_window=table_window)
+    return HeKit(ctx, key, dict(pk, key_bits=bits, **sec), schema)
 
 
 # Live kits by key, so that unpickled ciphertext arrays find an engine key
@@ -334,6 +344,15 @@ class HeKit:
         has_secret = all(key_ints.get(k) is not None for k in sec)
         self.secret_key = {k: key_ints[k] for k in sec} if has_secret else None
         _KITS[id(self)] = self
+
+    def public_key_bytes(self):
+        """PublicKey::Serialize with the schema value (HEU's key wire format)."""
+        return keywire.serialize_public_key(self.public_key, self.schema)
+
+    def secret_key_bytes(self):
+        if self.secret_key is None:
+            raise ValueError("this HeKit was set up from a public key and holds no secret key")
+        return keywire.serialize_secret_key(self.secret_key, self.n, self.schema)
 
     def array(self, values, encoder=None):
         """hnp.array(ndarray, encoder): values encoded by ``encoder`` when one
