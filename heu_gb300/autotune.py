@@ -57,7 +57,7 @@ def save(config, key_bits, path=DEFAULT_CACHE, device=0, rates=None):
         entry["rates"] = rates
     data.setdefault(device_name(device), {})[str(key_bits)] = entry
     os.makedirs(os.path.dirname(path) or ".", exist_ok=True)
-    tmp = path + ".tmp"
+    tmp = f"{path}.{os.getpid()}.tmp"  # processes saving at once each replace the file whole
     with open(tmp, "w") as f:
         json.dump(data, f, indent=1, sort_keys=True)
     os.replace(tmp, path)
