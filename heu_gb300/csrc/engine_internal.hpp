@@ -16,4 +16,8 @@ int key_view(hg_ctx* ctx, int key_id, KeyConst* kc, int* S, int* device, cudaStr
 // Records `msg` as the calling thread's last error (read by hg_last_error).
 void set_last_error(const char* msg);
 
+// Drops the cached device address of the allocation-free Sum's scratch array
+// for `device` (called when a context is created there).
+void forget_noalloc_scratch(int device);
+
 }  // namespace hg

@@ -35,7 +35,11 @@ constexpr int kMaxFirstChunk = 128;
 
 static __device__ __align__(256) uint32_t g_sum_scratch[kScratchBytes / sizeof(uint32_t)];
 
-// Device address of g_sum_scratch per device, resolved once per device.
+// Device address of g_sum_scratch per device, resolved by the first call on
+// that device (so that first call should come before any stream capture) and
+// dropped whenever an engine context is created on the device: a device reset
+// unloads the module and invalidates every context, and the new context's
+// first allocation-free call resolves the address again.
 uint32_t* g_scratch_addr[kMaxDevices] = {};
 std::mutex g_scratch_mu;
 
@@ -55,7 +59,29 @@ int scratch_address(int device, uint32_t** out) {
 
 size_t half_capacity(int S) { return (kScratchBytes - kHeadBytes) / (size_t)(4 * S) / 2; }
 
+// Puts the caller's current device back on every return path.
+struct RestoreDevice {
+  int device = -1;
+  RestoreDevice() {
+    if (cudaGetDevice(&device) != cudaSuccess) device = -1;
+  }
+  ~RestoreDevice() {
+    int now = -1;
+    if (device >= 0 && cudaGetDevice(&now) == cudaSuccess && now != device) cudaSetDevice(device);
+  }
+};
+
 }  // namespace
+
+namespace hg {
+
+void forget_noalloc_scratch(int device) {
+  if (device < 0 || device >= kMaxDevices) return;
+  std::lock_guard<std::mutex> lk(g_scratch_mu);
+  g_scratch_addr[device] = nullptr;
+}
+
+}  // namespace hg
 
 extern "C" int hg_dev_sum_noalloc(hg_ctx* ctx, int key_id, const uint32_t* a, size_t count, uint32_t* out,
                                   void* stream) {
@@ -82,6 +108,7 @@ extern "C" int hg_dev_sum_noalloc(hg_ctx* ctx, int key_id, const uint32_t* a, si
         "ciphertexts: 4,194,176 / 2,097,024 / 1,398,016 for 1024 / 2048 / 3072-bit keys); use hg_dev_sum");
     return HG_ERR_INVALID;
   }
+  const RestoreDevice keep;
   if (cudaSetDevice(device) != cudaSuccess) {
     hg::set_last_error("hg_dev_sum_noalloc: cudaSetDevice failed");
     return HG_ERR_CUDA;
@@ -107,7 +134,7 @@ extern "C" int hg_dev_sum_noalloc(hg_ctx* ctx, int key_id, const uint32_t* a, si
     size_t n = count;
     int which = 0;
     bool first = true;
-    const size_t target = (size_t)std::max(1, 152 * 4 * hg::instances_per_block(S, kc.variant));
+    const size_t target = (size_t)std::max(1, hg_device_sm_count(ctx) * 4 * hg::instances_per_block(S, kc.variant));
     while (n > 1 && ce == cudaSuccess) {
       size_t chunk;
       if (first) {

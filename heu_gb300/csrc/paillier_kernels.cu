@@ -89,6 +89,37 @@ __global__ void __launch_bounds__(kBlock) k_mul(KeyConst kc, const uint32_t* __r
   }
 }
 
+// Mul by multi-limb scalars; persistent like k_mul (one odd-power table of
+// 2^(wb-1) entries per instance slot of the grid).
+template <int TPI, int L>
+__global__ void __launch_bounds__(kBlock) k_mul_bn(KeyConst kc, const uint32_t* __restrict__ a,
+                                                   const uint32_t* __restrict__ emag, int el,
+                                                   uint32_t* __restrict__ out, size_t count,
+                                                   uint32_t* __restrict__ scratch, int wb, uint32_t* err,
+                                                   unsigned long long* ctr) {
+  constexpr int S = TPI * L;
+  constexpr int IPB = kBlock / TPI;
+  constexpr int IPW = 32 / TPI;
+  const Group<TPI> g;
+  const int lane_inst = (threadIdx.x & 31) / TPI;
+  const int warp_first = (threadIdx.x >> 5) * IPW;
+  const int ntab = 1 << (wb - 1);
+  uint32_t* tb = scratch + ((size_t)blockIdx.x * IPB + warp_first + lane_inst) * (size_t)ntab * S + g.t * L;
+  uint32_t N[L];
+  load_slice<L>(N, kc.N + g.t * L);
+  for (size_t wbase = next_work(ctr, IPW); wbase < count; wbase = next_work(ctr, IPW)) {
+    const size_t inst = wbase + lane_inst;
+    const bool active = inst < count;
+    mul_bn_one<TPI, L>(kc, a, emag, el, out, active ? inst : count - 1, active, tb, wb, N, g, err);
+  }
+}
+
+// sel[i] = -1 where neg[i] != 0, else 1 (the inverse's selector)
+__global__ void k_sel_from_neg(const uint8_t* __restrict__ neg, int64_t* __restrict__ sel, size_t count) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count) sel[i] = neg[i] ? -1 : 1;
+}
+
 // Chunked product reduction: out[j] = prod in[j*chunk .. (j+1)*chunk)
 // (numpy/evaluator.cc:355-373 reduces with AddInplace = MulMod)
 template <int TPI, int L>
@@ -109,6 +140,8 @@ __global__ void __launch_bounds__(kBlock) k_reduce(KeyConst kc, const uint32_t* 
     if (!__any_sync(kFull, valid)) break;
     uint32_t B[L];
     load_slice<L>(B, (valid ? in + idx * S : kc.R1) + g.t * L);
+    // every input is range-checked before it enters mont_mul (b < N)
+    check_ct<TPI, L>(B, N, active && valid, g, err);
     mont_mul<TPI, L>(acc, acc, B, N, kc.np, g);
   }
   if (active) store_slice<L>(out + i * S + g.t * L, acc);
@@ -316,6 +349,33 @@ cudaError_t launch_mul(int S, const KeyConst& kc, const uint32_t* a, const int64
     const unsigned gb = (unsigned)std::min((size_t)need, (size_t)grid);
     k_mul<TPI, L><<<gb, kBlock, 0, st>>>(kc, a, k, out, count, scratch, wm, err, ctr);
   });
+  return counted();
+}
+
+cudaError_t launch_mul_bn(int S, const KeyConst& kc, const uint32_t* a, const uint32_t* emag, int el,
+                          uint32_t* out, size_t count, uint32_t* scratch, int wb, uint32_t* err, int grid,
+                          unsigned long long* ctr, cudaStream_t st) {
+  if (count == 0) return cudaSuccess;
+  if (el < 1 || wb < 1 || wb > 8) return cudaErrorInvalidValue;
+  const cudaError_t e = cudaMemsetAsync(ctr, 0, sizeof(*ctr), st);
+  if (e != cudaSuccess) return e;
+  HG_DISPATCH_S0(S, {
+    const unsigned need = blocks_for(count, TPI);
+    const unsigned gb = (unsigned)std::min((size_t)need, (size_t)grid);
+    k_mul_bn<TPI, L><<<gb, kBlock, 0, st>>>(kc, a, emag, el, out, count, scratch, wb, err, ctr);
+  });
+  return counted();
+}
+
+int resident_blocks_mul_bn(int S) {
+  int r = 0;
+  [&]() -> cudaError_t { HG_DISPATCH_S0(S, r = occupancy_blocks(k_mul_bn<TPI, L>)); return cudaSuccess; }();
+  return r;
+}
+
+cudaError_t launch_sel_from_neg(const uint8_t* neg, int64_t* sel, size_t count, cudaStream_t st) {
+  if (count == 0) return cudaSuccess;
+  k_sel_from_neg<<<(unsigned)((count + 255) / 256), 256, 0, st>>>(neg, sel, count);
   return counted();
 }
 

@@ -62,3 +62,25 @@ def test_noalloc_sum_rejects_counts_beyond_its_scratch(gpu_key):
     out = torch.zeros((1, key.ct_limbs), dtype=torch.int32, device="cuda")
     rc = key.lib.hg_dev_sum_noalloc(key.ctx.handle, key.id, _ptr(bad), 2, _ptr(out), None)
     assert rc == capi.HG_ERR_CT_RANGE
+
+
+def test_noalloc_sum_checks_every_input(gpu_key):
+    """One value >= n^2 anywhere in the input, not only at the start of a
+    reduction chunk, is rejected; a valid call right after still sums."""
+    torch = pytest.importorskip("torch")
+    key, pk, sk = gpu_key(2048, 0)
+    lib, h = key.lib, key.ctx.handle
+    m, ct = _encrypt_on_device(torch, key, 300_000, 7)
+    n2 = torch.from_numpy(hg.ints_to_limbs([pk.n2 + 3], key.ct_limbs).view(np.int32)).cuda()
+    out = torch.zeros((1, key.ct_limbs), dtype=torch.int32, device="cuda")
+    for n, bad_at in ((2, 1), (64, 63), (300_000, 1), (300_000, 12_345)):
+        x = ct[:n].clone()
+        x[bad_at] = n2[0]
+        rc = lib.hg_dev_sum_noalloc(h, key.id, _ptr(x), n, _ptr(out), None)
+        assert rc == capi.HG_ERR_CT_RANGE, (n, bad_at)
+    want = torch.zeros_like(out)
+    capi.check(lib.hg_dev_sum(h, key.id, _ptr(ct), 300_000, _ptr(want), None))
+    torch.cuda.synchronize()
+    capi.check(lib.hg_dev_check(h))
+    capi.check(lib.hg_dev_sum_noalloc(h, key.id, _ptr(ct), 300_000, _ptr(out), None))
+    assert torch.equal(out, want)
