@@ -155,6 +155,49 @@ def cpu_sample(seconds_hint=10.0, threads=None):
     return rates, step_rate, threads, sample
 
 
+def parity_sample(kp, m, r, kk, ct, cm, cs, ct2, count=4096):
+    """Checker only, after the timed region: a strided sample of the timed
+    outputs (Encrypt at the bench's table window, Add, Mul by 64-bit k)
+    compared byte for byte, in Montgomery form, with the paillier_z C
+    restatement given the same m, r and k.  Returns the number of
+    ciphertexts compared; raises on any mismatch."""
+    import numpy as np
+
+    from oracle import cref
+    from oracle import paillier_z as pz
+
+    n = ct.shape[0]
+    step = max(1, n // count)
+    idx = np.arange(0, n, step)[:count]
+    # include the last element as well (strided samples may miss the tail)
+    idx[-1] = n - 1
+    pk, sk = pz.keygen(KEY_BITS, KEY_SEED)
+    assert pk.n == kp["n"], "bench key differs from the oracle key"
+    ck = cref.CKey(KEY_BITS, pk, sk, window=10)
+    threads = os.cpu_count() or 1
+    ti = __import__("torch").from_numpy(idx).to(ct.device)
+    mh = m[ti].cpu().numpy()
+    rh = np.ascontiguousarray(r[ti].cpu().numpy().view(np.uint32)).view(np.uint64)
+    kh = kk[ti].cpu().numpy()
+
+    def u32(t):
+        return np.ascontiguousarray(t[ti].cpu().numpy().view(np.uint32))
+
+    want_ct = ck.encrypt(mh, rh, threads)
+    got = u32(ct)
+    bad = int((got != want_ct.view(np.uint32).reshape(got.shape)).any(axis=1).sum())
+    assert bad == 0, f"encrypt parity: {bad} of {idx.size} sampled ciphertexts differ from paillier_z"
+    want_cm = ck.mul(np.ascontiguousarray(want_ct), kh, threads)
+    got = u32(cm)
+    bad = int((got != want_cm.view(np.uint32).reshape(got.shape)).any(axis=1).sum())
+    assert bad == 0, f"mul parity: {bad} of {idx.size} sampled ciphertexts differ from paillier_z"
+    want_cs = ck.add(np.ascontiguousarray(want_ct), np.ascontiguousarray(u32(ct2)).view(np.uint64), threads)
+    got = u32(cs)
+    bad = int((got != want_cs.view(np.uint32).reshape(got.shape)).any(axis=1).sum())
+    assert bad == 0, f"add parity: {bad} of {idx.size} sampled ciphertexts differ from paillier_z"
+    return int(idx.size) * 3
+
+
 def reference_arm(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -335,6 +378,10 @@ def ours_arm(args):
         mh, kh = m[idx].cpu().tolist(), kk[idx].cpu().tolist()
         assert got == [a * b for a, b in zip(mh, kh)], "mul spot check mismatch"
 
+    parity_checked = 0
+    if len(ops) == 4 and not args.no_parity:
+        parity_checked = parity_sample(kp, m, r, kk, ct, cm, cs, ct2)
+
     value = len(ops) * n * world * args.steps / elapsed
     per_op = {nm: n * args.steps / op_s[nm] for nm in names if nm in ops}
     if "mul" in ops:
@@ -498,6 +545,10 @@ def ours_arm(args):
                                         "patterns); MEASURED_PEAKS.json has no integer figure",
                          "peak_chain_pattern": peak_chain, "peak_wide_pattern": peak_wide,
                          "per_op_tmacs": roof_ops},
+            "parity_checked": parity_checked,
+            "parity": ("strided sample of the timed Encrypt / Add / Mul outputs byte-equal (Montgomery form) to "
+                       "the paillier_z C restatement given the same m, r, k; every timed decryption equal to "
+                       "m + m2"),
             "e2e": e2e,
             "small_call_us": small,
             "cpu_baseline": cpu,
@@ -1176,6 +1227,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-parity", action="store_true", help="skip the post-timing byte comparison with paillier_z")
     ap.add_argument("--workload", choices=["config2", "config3", "config4", "config5", "ou", "wire"],
                     default="config2")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner")

@@ -60,6 +60,7 @@ SIGNATURES = {
     "hg_sub_plain": [_P, _I, _P, _P, _P, _SZ],
     "hg_plain_sub": [_P, _I, _P, _P, _P, _SZ],
     "hg_mul": [_P, _I, _P, _P, _P, _SZ],
+    "hg_mul_bn": [_P, _I, _P, _P, _P, _SZ, _P, _SZ],
     "hg_negate": [_P, _I, _P, _P, _SZ],
     "hg_sum": [_P, _I, _P, _SZ, _P],
     "hg_to_mont": [_P, _I, _P, _P, _SZ],
@@ -68,6 +69,7 @@ SIGNATURES = {
     "hg_dev_decrypt": [_P, _I, _P, _P, _P, _SZ, _P],
     "hg_dev_add": [_P, _I, _P, _P, _P, _SZ, _P],
     "hg_dev_mul": [_P, _I, _P, _P, _P, _SZ, _P],
+    "hg_dev_mul_bn": [_P, _I, _P, _P, _P, _SZ, _P, _SZ, _P],
     "hg_dev_sum": [_P, _I, _P, _SZ, _P, _P],
     "hg_dev_encrypt_zero": [_P, _I, _P, _P, _SZ, _P],
     "hg_dev_randomize": [_P, _I, _P, _P, _SZ, _P],
@@ -88,6 +90,8 @@ SIGNATURES = {
     "hg_dev_bucket_sum": [_P, _I, _P, _SZ, _SZ, _P, _SZ, _I, _I, _P, _P],
     "hg_matmul": [_P, _I, _P, _SZ, _SZ, _P, _SZ, _P],
     "hg_dev_matmul": [_P, _I, _P, _SZ, _SZ, _P, _SZ, _P, _P],
+    "hg_matmul_bn": [_P, _I, _P, _SZ, _SZ, _P, _P, _SZ, _SZ, _P],
+    "hg_dev_matmul_bn": [_P, _I, _P, _SZ, _SZ, _P, _P, _SZ, _SZ, _P, _P],
     "hg_key_get_config": [_P, _I, _P],
     "hg_key_set_config": [_P, _I, _P],
     "hg_autotune": [_P, _I, _SZ, _P, _P],

@@ -5,7 +5,8 @@
 // heu/library/algorithms/paillier_zahlen (keys, Ciphertext) and of the
 // vectorized SPI templates heu/library/algorithms/clean_template/
 // vector_encryptor.h:24-33, vector_decryptor.h:25-31, vector_evaluator.h:24-66,
-// so that a HEU build registers it as a new schema.  Outside
+// so that a HEU build registers it as a new schema at the five points of
+// heu/library/phe/base/schema.h:31-100 and schema.cc:35-64.  Outside
 // HEU, `BigInt` and `Span` below are small stand-ins for yacl::math::BigInt
 // and absl::Span<T* const>; inside HEU they are replaced by those types.
 //
@@ -15,6 +16,7 @@
 // bookkeeping run on the host.
 #pragma once
 
+#include <algorithm>
 #include <cstdint>
 #include <cstring>
 #include <map>
@@ -488,19 +490,34 @@ class Evaluator {
   void SubInplace(Span<Ciphertext> a, ConstSpan<Plaintext> b) const { Assign(a, Sub(Const(a), b)); }
   void SubInplace(Span<Plaintext> a, ConstSpan<Plaintext> b) const { AssignP(a, Sub(ConstP(a), b)); }
 
-  // evaluator.cc:99-123 (scalars must fit int64)
+  // evaluator.cc:99-123: scalars of any size up to the width of n^2 (int64
+  // scalars take hg_mul, wider ones hg_mul_bn)
   std::vector<Ciphertext> Mul(ConstSpan<Ciphertext> a, ConstSpan<Plaintext> b) const {
     SameSize(a.size(), b.size());
     const auto x = detail::CtLimbs(pk_, a);
-    std::vector<int64_t> k(b.size());
-    for (size_t i = 0; i < b.size(); ++i) {
-      if (b[i]->BitCount() > 63 && !(b[i]->IsNegative() && b[i]->BitCount() == 64 &&
-                                     b[i]->Mag() == hg::BN(1ull << 63)))
-        throw std::invalid_argument("GB300 Paillier: scalar does not fit int64");
-      k[i] = b[i]->Get<int64_t>();
-    }
     std::vector<uint32_t> out(x.size());
-    detail::Check(hg_mul(ctx(), id(), x.data(), k.data(), out.data(), a.size()));
+    size_t bits = 0;
+    bool fits = true;
+    for (size_t i = 0; i < b.size(); ++i) {
+      bits = std::max(bits, b[i]->BitCount());
+      fits &= b[i]->BitCount() <= 63 ||
+              (b[i]->IsNegative() && b[i]->BitCount() == 64 && b[i]->Mag() == hg::BN(1ull << 63));
+    }
+    if (fits) {
+      std::vector<int64_t> k(b.size());
+      for (size_t i = 0; i < b.size(); ++i) k[i] = b[i]->Get<int64_t>();
+      detail::Check(hg_mul(ctx(), id(), x.data(), k.data(), out.data(), a.size()));
+    } else {
+      const size_t kl = (bits + 31) / 32;
+      if (kl > pk_.Limbs()) throw std::invalid_argument("GB300 Paillier: scalar wider than n^2");
+      std::vector<uint32_t> mag(b.size() * kl);
+      std::vector<uint8_t> neg(b.size());
+      for (size_t i = 0; i < b.size(); ++i) {
+        b[i]->Mag().to_limbs(mag.data() + i * kl, kl);
+        neg[i] = b[i]->IsNegative() ? 1 : 0;
+      }
+      detail::Check(hg_mul_bn(ctx(), id(), x.data(), mag.data(), neg.data(), kl, out.data(), a.size()));
+    }
     return detail::ToCts(out, pk_.Limbs());
   }
   std::vector<Ciphertext> Mul(ConstSpan<Plaintext> a, ConstSpan<Ciphertext> b) const { return Mul(b, a); }

@@ -55,9 +55,24 @@ struct NvtxRange {
   ~NvtxRange() { nvtxRangePop(); }
 };
 
+// The calling thread's current CUDA device, put back when a C-ABI call
+// returns: the engine switches to its context's device, and a caller that
+// works on another device must not find its own selection changed.
+struct CurrentDeviceKeeper {
+  int device = -1;
+  CurrentDeviceKeeper() {
+    if (cudaGetDevice(&device) != cudaSuccess) device = -1;
+  }
+  ~CurrentDeviceKeeper() {
+    int now = -1;
+    if (device >= 0 && cudaGetDevice(&now) == cudaSuccess && now != device) cudaSetDevice(device);
+  }
+};
+
 template <typename F>
 int guarded(const char* name, F&& f) {
   NvtxRange range(name);
+  const CurrentDeviceKeeper keep;
   try {
     return f();
   } catch (const HgError& e) {
@@ -161,6 +176,7 @@ struct KeyRec {
   hg::KeyConst kc{};
   hg::SecConst sc{};
   int grid_mul = 0, grid_dec = 0;
+  int grid_mul_bn = 0;  // persistent grid of the multi-limb scalar Mul (set on first use)
   int wm = 4;  // scalar-mul window
   // Okamoto-Uchiyama keys (scheme 1): kc is over n with the H table; kcG /
   // kcGi hold the G and G^-1 tables; oc the decryption constants
@@ -237,7 +253,8 @@ struct Work {
   DevBuf scratch, red[2];
   TreeBufs inv;
   DevBuf seg_cnt, seg_offs[3], seg_cursor, seg_idx, seg_nch, seg_part[2];
-  DevBuf mm_tables, mm_masks, mm_prod;
+  DevBuf mm_tables, mm_masks, mm_prod, mm_exp;
+  DevBuf sel;  // signs of multi-limb scalars as the inverse's selector
   DevBuf ou_e[2];
   DevBuf err;
   PinBuf pin_root, pin_err, pin_z, pin_wire;
@@ -566,10 +583,58 @@ void core_mul(KeyRec& k, Work& w, const uint32_t* a, const int64_t* kk, const in
   }
 }
 
+// Sliding-window width for exponents of at most `bits` bits: the w in 1..8
+// with the fewest multiplications, bits / (w + 1) window products plus the
+// 2^(w-1) odd powers of the table.
+int bn_window(size_t bits) {
+  int best = 1;
+  double cost = 1e300;
+  for (int w = 1; w <= 8; ++w) {
+    const double c = (double)bits / (w + 1) + (double)(1 << (w - 1));
+    if (c < cost) {
+      cost = c;
+      best = w;
+    }
+  }
+  return best;
+}
+
+// Mul(ct, k) for multi-limb scalars (evaluator.cc:99-123): magnitudes emag
+// (el limbs each) and signs eneg on the device; max_bits bounds the
+// magnitudes (it sets the window); any_neg = false skips the inverse.
+void core_mul_bn(KeyRec& k, Work& w, const uint32_t* a, const uint32_t* emag, int el, const uint8_t* eneg,
+                 size_t max_bits, bool any_neg, uint32_t* out, size_t count, bool sync_inverse = true) {
+  if (el < 1 || el > k.S) fail(HG_ERR_INVALID, "scalar limbs must be in [1, S] (at most the width of n^2)");
+  if (count == 0) return;
+  const int wb = bn_window(std::max<size_t>(max_bits, 1));
+  if (k.grid_mul_bn == 0) k.grid_mul_bn = hg::resident_blocks_mul_bn(k.S);
+  const size_t inst = (size_t)k.grid_mul_bn * hg::instances_per_block(k.S, 0);
+  uint32_t* scratch = w.scratch.ensure<uint32_t>(inst * ((size_t)1 << (wb - 1)) * k.S * 4);
+  cuda_check(hg::launch_mul_bn(k.S, k.kc, a, emag, el, out, count, scratch, wb, w.errp(), k.grid_mul_bn, w.ctrp(),
+                               w.stream),
+             "mul_bn launch");
+  if (any_neg) {
+    int64_t* sel = w.sel.ensure<int64_t>(count * 8);
+    cuda_check(hg::launch_sel_from_neg(eneg, sel, count, w.stream), "sign selector");
+    if (sync_inverse)
+      core_inverse(k, w, out, sel, out, count);
+    else
+      core_inverse_enqueue(k, w, out, sel, out, count);
+  }
+}
+
+// Multiprocessors of the current device (the caller has selected it).
+int current_sm_count() {
+  int dev = 0, sms = 0;
+  cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+  cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "attr");
+  return sms;
+}
+
 void core_sum(KeyRec& k, Work& w, const uint32_t* a, size_t count, uint32_t* out) {
   if (count == 0) fail(HG_ERR_INVALID, "you cannot sum an empty tensor");
   const size_t S = (size_t)k.S;
-  const size_t target = (size_t)std::max(1, 152 * 4 * hg::instances_per_block(k.S, k.kc.variant));
+  const size_t target = (size_t)std::max(1, current_sm_count() * 4 * hg::instances_per_block(k.S, k.kc.variant));
   const uint32_t* cur = a;
   size_t n = count;
   int which = 0;
@@ -634,20 +699,12 @@ void core_bucket_sum(KeyRec& k, Work& w, const uint32_t* x, size_t rows, size_t 
 }
 
 // numpy MatMul of ciphertexts x (M x K) by int64 plaintexts y (K x N, host).
-void core_matmul(KeyRec& k, Work& w, const uint32_t* x, size_t M, size_t K, const int64_t* y, size_t N,
-                 uint32_t* out) {
-  if (M == 0 || K == 0 || N == 0) fail(HG_ERR_INVALID, "HEU does not support empty tensor currently");
-  if (K > (1u << 20) || N > (1u << 20)) fail(HG_ERR_INVALID, "matmul dimension too large");
-  int64_t ymin = y[0], ymax = y[0];
-  for (size_t i = 1; i < K * N; ++i) {
-    ymin = std::min(ymin, y[i]);
-    ymax = std::max(ymax, y[i]);
-  }
-  // shift to y' = y + o >= 0; undo with (prod_k x(i,k))^-o per row
-  const uint64_t o = ymin < 0 ? (uint64_t)0 - (uint64_t)ymin : 0;
-  const uint64_t ymax_s = (uint64_t)ymax + o;
-  int P = 1;
-  while (P < 64 && (ymax_s >> P) != 0) ++P;
+// MatMul over exponents given as bit planes: bit(kk, j, plane) is bit `plane`
+// of y'(kk, j) = y(kk, j) + o >= 0 (P planes); o >= 0 is undone per row with
+// (prod_k x(i,k))^-o.
+template <typename Bit>
+void core_matmul_planes(KeyRec& k, Work& w, const uint32_t* x, size_t M, size_t K, size_t N, int P, Bit&& bit,
+                        const BN& o, uint32_t* out) {
   const int nch = (int)((K + 7) / 8);
   std::vector<uint8_t> hm((size_t)N * P * nch, 0);
   for (size_t j = 0; j < N; ++j)
@@ -656,12 +713,19 @@ void core_matmul(KeyRec& k, Work& w, const uint32_t* x, size_t M, size_t K, cons
         uint8_t mk = 0;
         for (int b = 0; b < 8; ++b) {
           const size_t kk = (size_t)c * 8 + b;
-          if (kk < K && ((((uint64_t)y[kk * N + j] + o) >> plane) & 1ull)) mk |= (uint8_t)(1u << b);
+          if (kk < K && bit(kk, j, plane)) mk |= (uint8_t)(1u << b);
         }
         hm[((size_t)j * P + plane) * nch + c] = mk;
       }
   uint8_t* dmask = w.mm_masks.ensure<uint8_t>(hm.size());
   cuda_check(cudaMemcpyAsync(dmask, hm.data(), hm.size(), cudaMemcpyHostToDevice, w.stream), "H2D masks");
+  // o as exponent limbs on the device (only used when it does not fit 64 bits)
+  const std::vector<uint32_t> ol = o.limbs(std::max<size_t>(1, (o.bitlen() + 31) / 32));
+  uint32_t* dexp = nullptr;
+  if (o.bitlen() > 64) {
+    dexp = w.mm_exp.ensure<uint32_t>(ol.size() * 4);
+    cuda_check(cudaMemcpyAsync(dexp, ol.data(), ol.size() * 4, cudaMemcpyHostToDevice, w.stream), "H2D exponent");
+  }
   const size_t per_row = hg::subset_table_bytes_per_row(k.S, (int)K);
   const size_t budget = (size_t)8 << 30;
   const size_t Rb = std::max<size_t>(1, std::min(M, budget / per_row));
@@ -672,15 +736,66 @@ void core_matmul(KeyRec& k, Work& w, const uint32_t* x, size_t M, size_t K, cons
     cuda_check(hg::launch_subset_tables(k.S, k.kc, x, r0, rows, (int)K, T, w.errp(), w.stream), "subset tables");
     cuda_check(hg::launch_matmul_planes(k.S, k.kc, T, dmask, r0, rows, (int)N, P, (int)K, out, w.stream),
                "matmul planes");
-    if (o > 0) {
+    if (!o.is_zero()) {
       cuda_check(hg::launch_row_products(k.S, k.kc, T, rows, (int)K, prod, w.stream), "row products");
       core_inverse(k, w, prod, nullptr, prod, rows);
-      cuda_check(hg::launch_pow_shared(k.S, k.kc, prod, rows, o, w.stream), "row power");
+      if (dexp)
+        cuda_check(hg::launch_pow_shared_bn(k.S, k.kc, prod, rows, dexp, (int)ol.size(), w.stream), "row power");
+      else
+        cuda_check(hg::launch_pow_shared(k.S, k.kc, prod, rows, o.low64(), w.stream), "row power");
       cuda_check(hg::launch_scale_rows(k.S, k.kc, out, prod, r0, rows, (int)N, w.stream), "scale rows");
     }
   }
-  // keep the host mask array alive until its copy has run
+  // keep the host mask and exponent arrays alive until their copies have run
   cuda_check(cudaStreamSynchronize(w.stream), "stream sync");
+}
+
+void check_matmul_dims(size_t M, size_t K, size_t N) {
+  if (M == 0 || K == 0 || N == 0) fail(HG_ERR_INVALID, "HEU does not support empty tensor currently");
+  if (K > (1u << 20) || N > (1u << 20)) fail(HG_ERR_INVALID, "matmul dimension too large");
+}
+
+void core_matmul(KeyRec& k, Work& w, const uint32_t* x, size_t M, size_t K, const int64_t* y, size_t N,
+                 uint32_t* out) {
+  check_matmul_dims(M, K, N);
+  int64_t ymin = y[0], ymax = y[0];
+  for (size_t i = 1; i < K * N; ++i) {
+    ymin = std::min(ymin, y[i]);
+    ymax = std::max(ymax, y[i]);
+  }
+  // shift to y' = y + o >= 0; undo with (prod_k x(i,k))^-o per row
+  const uint64_t o = ymin < 0 ? (uint64_t)0 - (uint64_t)ymin : 0;
+  const uint64_t ymax_s = (uint64_t)ymax + o;
+  int P = 1;
+  while (P < 64 && (ymax_s >> P) != 0) ++P;
+  core_matmul_planes(k, w, x, M, K, N, P,
+                     [&](size_t kk, size_t j, int plane) { return ((((uint64_t)y[kk * N + j] + o) >> plane) & 1ull) != 0; },
+                     BN(o), out);
+}
+
+// MatMul with plaintext entries of any size (numpy/evaluator.cc:208-353 takes
+// any PMatrix): y(kk, j) = (neg ? -1 : 1) * magnitude of yl limbs.
+void core_matmul_bn(KeyRec& k, Work& w, const uint32_t* x, size_t M, size_t K, const uint32_t* y_mag,
+                    const uint8_t* y_neg, size_t yl, size_t N, uint32_t* out) {
+  check_matmul_dims(M, K, N);
+  if (yl < 1 || yl > (size_t)k.S) fail(HG_ERR_INVALID, "plaintext limbs must be in [1, S]");
+  const size_t cnt = K * N;
+  std::vector<BN> mag(cnt);
+  BN o(0);
+  for (size_t i = 0; i < cnt; ++i) {
+    mag[i] = BN::from_limbs(y_mag + i * yl, yl);
+    if (y_neg[i] && !mag[i].is_zero() && mag[i] > o) o = mag[i];
+  }
+  // y' = y + o: o - |y| for negative entries, o + |y| otherwise
+  std::vector<BN> ys(cnt);
+  size_t P = 1;
+  for (size_t i = 0; i < cnt; ++i) {
+    ys[i] = (y_neg[i] && !mag[i].is_zero()) ? o - mag[i] : o + mag[i];
+    P = std::max(P, ys[i].bitlen());
+  }
+  if (P > 32 * (size_t)k.S + 1) fail(HG_ERR_INVALID, "plaintext too wide");
+  core_matmul_planes(k, w, x, M, K, N, (int)P,
+                     [&](size_t kk, size_t j, int plane) { return ys[kk * N + j].bit((size_t)plane); }, o, out);
 }
 
 int load_key(hg_ctx* ctx, uint32_t key_bits, const uint32_t* n_l, const uint32_t* hs_l, const uint32_t* p_l,
@@ -1036,6 +1151,7 @@ int hg_ctx_create(int device, hg_ctx** out) {
     auto ctx = std::make_unique<hg_ctx>();
     ctx->device = device;
     cuda_check(cudaSetDevice(device), "cudaSetDevice");
+    hg::forget_noalloc_scratch(device);
     cuda_check(cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device), "attr");
     for (int i = 0; i < kLanes; ++i) {
       auto w = std::make_unique<Work>();
@@ -1451,6 +1567,39 @@ int hg_mul(hg_ctx* ctx, int key_id, const uint32_t* a, const int64_t* kk, uint32
   });
 }
 
+int hg_mul_bn(hg_ctx* ctx, int key_id, const uint32_t* a, const uint32_t* k_mag, const uint8_t* k_neg,
+              size_t k_limbs, uint32_t* out, size_t count) {
+  return guarded(__func__, [&] {
+    if (!a || !k_mag || !k_neg || !out) fail(HG_ERR_INVALID, "null argument");
+    HG_HOST_PROLOGUE
+    if (k_limbs < 1 || k_limbs > (size_t)k->S) fail(HG_ERR_INVALID, "scalar limbs must be in [1, S] (at most the width of n^2)");
+    size_t max_bits = 0;
+    bool any_neg = false;
+    for (size_t i = 0; i < count; ++i) {
+      const uint32_t* e = k_mag + i * k_limbs;
+      size_t l = k_limbs;
+      while (l > 0 && e[l - 1] == 0u) --l;
+      if (l == 0) continue;
+      size_t b = 32 * (l - 1);
+      for (uint32_t t = e[l - 1]; t; t >>= 1) ++b;
+      max_bits = std::max(max_bits, b);
+      any_neg |= k_neg[i] != 0;
+    }
+    run_chunked(ctx, w, count, [&](Work& v, size_t off, size_t cnt) {
+      auto* da = v.io[0].ensure<uint32_t>(cnt * cb);
+      auto* dk = v.io[1].ensure<uint32_t>(cnt * k_limbs * 4);
+      auto* dout = v.io[2].ensure<uint32_t>(cnt * cb);
+      auto* dn = v.io[3].ensure<uint8_t>(cnt);
+      h2d(da, (const uint8_t*)a + off * cb, cnt * cb, v);
+      h2d(dk, k_mag + off * k_limbs, cnt * k_limbs * 4, v);
+      h2d(dn, k_neg + off, cnt, v);
+      core_mul_bn(*k, v, da, dk, (int)k_limbs, dn, max_bits, any_neg, dout, cnt, false);
+      d2h((uint8_t*)out + off * cb, dout, cnt * cb, v);
+    }, [](Work& v) { v.task.status = 0; }, [](Work& v) { raise_task_status(v.task); });
+    return HG_OK;
+  });
+}
+
 // ---------------------------------------------------------------------------
 // HEU wire format for ciphertext matrices (numpy/matrix.h:221-310); the items
 // are packed and unpacked by the kernels in wire_kernels.cu, the msgpack
@@ -1709,6 +1858,17 @@ int hg_dev_mul(hg_ctx* ctx, int key_id, const uint32_t* a, const int64_t* kk, ui
   });
 }
 
+int hg_dev_mul_bn(hg_ctx* ctx, int key_id, const uint32_t* a, const uint32_t* k_mag, const uint8_t* k_neg,
+                  size_t k_limbs, uint32_t* out, size_t count, void* stream) {
+  return guarded(__func__, [&] {
+    HG_DEV_PROLOGUE
+    // the magnitudes stay on the device: the window follows their width and
+    // the inverse runs with the signs as its selector
+    core_mul_bn(*k, w, a, k_mag, (int)k_limbs, k_neg, 32 * k_limbs, true, out, count);
+    return HG_OK;
+  });
+}
+
 int hg_dev_encrypt_zero(hg_ctx* ctx, int key_id, const uint32_t* r, uint32_t* ct_out, size_t count, void* stream) {
   return guarded(__func__, [&] {
     HG_DEV_PROLOGUE
@@ -1849,6 +2009,35 @@ int hg_dev_matmul(hg_ctx* ctx, int key_id, const uint32_t* x, size_t M, size_t K
     if (count == 0 || N == 0) fail(HG_ERR_INVALID, "HEU does not support empty tensor currently");
     HG_DEV_PROLOGUE
     core_matmul(*k, w, x, M, K, y, N, out);
+    return HG_OK;
+  });
+}
+
+int hg_matmul_bn(hg_ctx* ctx, int key_id, const uint32_t* x, size_t M, size_t K, const uint32_t* y_mag,
+                 const uint8_t* y_neg, size_t y_limbs, size_t N, uint32_t* out) {
+  return guarded(__func__, [&] {
+    if (!x || !y_mag || !y_neg || !out) fail(HG_ERR_INVALID, "null argument");
+    const size_t count = M * K;
+    if (count == 0 || N == 0) fail(HG_ERR_INVALID, "HEU does not support empty tensor currently");
+    HG_HOST_PROLOGUE
+    auto* dx = w.io[0].ensure<uint32_t>(count * cb);
+    auto* dout = w.io[1].ensure<uint32_t>(M * N * cb);
+    h2d(dx, x, count * cb, w);
+    core_matmul_bn(*k, w, dx, M, K, y_mag, y_neg, y_limbs, N, dout);
+    d2h(out, dout, M * N * cb, w);
+    finish(w);
+    return HG_OK;
+  });
+}
+
+int hg_dev_matmul_bn(hg_ctx* ctx, int key_id, const uint32_t* x, size_t M, size_t K, const uint32_t* y_mag,
+                     const uint8_t* y_neg, size_t y_limbs, size_t N, uint32_t* out, void* stream) {
+  return guarded(__func__, [&] {
+    if (!y_mag || !y_neg) fail(HG_ERR_INVALID, "null argument");
+    const size_t count = M * K;
+    if (count == 0 || N == 0) fail(HG_ERR_INVALID, "HEU does not support empty tensor currently");
+    HG_DEV_PROLOGUE
+    core_matmul_bn(*k, w, x, M, K, y_mag, y_neg, y_limbs, N, out);
     return HG_OK;
   });
 }

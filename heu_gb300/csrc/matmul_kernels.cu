@@ -146,6 +146,35 @@ __global__ void __launch_bounds__(kBlock) k_pow_shared(KeyConst kc, uint32_t* __
   if (active) store_slice<L>(v + i * S + g.t * L, acc);
 }
 
+// v[i] = v[i]^e for one multi-limb exponent e >= 1 (el limbs, device memory)
+// shared by all instances: left-to-right square-and-multiply
+template <int TPI, int L>
+__global__ void __launch_bounds__(kBlock) k_pow_shared_bn(KeyConst kc, uint32_t* __restrict__ v, size_t count,
+                                                          const uint32_t* __restrict__ e, int el) {
+  constexpr int S = TPI * L;
+  const Group<TPI> g;
+  const size_t inst = ((size_t)blockIdx.x * kBlock + threadIdx.x) / TPI;
+  const size_t wfirst = ((size_t)blockIdx.x * kBlock + (threadIdx.x & ~31u)) / TPI;
+  if (wfirst >= count) return;
+  const bool active = inst < count;
+  const size_t i = active ? inst : count - 1;
+  int top = -1;
+#pragma unroll 1
+  for (int l = el - 1; l >= 0 && top < 0; --l)
+    if (e[l] != 0u) top = l * 32 + 31 - __clz(e[l]);
+  if (top < 0) return;  // e = 0 is not passed by the host
+  uint32_t N[L], x[L], acc[L];
+  load_slice<L>(N, kc.N + g.t * L);
+  load_slice<L>(x, v + i * S + g.t * L);
+  copy_slice<L>(acc, x);
+#pragma unroll 1
+  for (int bit = top - 1; bit >= 0; --bit) {
+    mont_mul<TPI, L>(acc, acc, acc, N, kc.np, g);
+    if ((e[bit >> 5] >> (bit & 31)) & 1u) mont_mul<TPI, L>(acc, acc, x, N, kc.np, g);
+  }
+  if (active) store_slice<L>(v + i * S + g.t * L, acc);
+}
+
 // out(r0 + i, j) *= q[i]
 template <int TPI, int L>
 __global__ void __launch_bounds__(kBlock) k_scale_rows(KeyConst kc, uint32_t* __restrict__ out,
@@ -208,6 +237,13 @@ cudaError_t launch_row_products(int S, const KeyConst& kc, const uint32_t* T, si
 cudaError_t launch_pow_shared(int S, const KeyConst& kc, uint32_t* v, size_t count, uint64_t e, cudaStream_t st) {
   if (e <= 1) return cudaSuccess;
   HG_DISPATCH_S3(S, k_pow_shared<TPI, L><<<nblocks(count, TPI), kBlock, 0, st>>>(kc, v, count, e));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pow_shared_bn(int S, const KeyConst& kc, uint32_t* v, size_t count, const uint32_t* e, int el,
+                                 cudaStream_t st) {
+  if (count == 0 || el < 1) return cudaSuccess;
+  HG_DISPATCH_S3(S, k_pow_shared_bn<TPI, L><<<nblocks(count, TPI), kBlock, 0, st>>>(kc, v, count, e, el));
   return cudaGetLastError();
 }
 

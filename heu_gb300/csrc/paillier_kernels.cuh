@@ -89,6 +89,15 @@ cudaError_t launch_add_plain(int S, const KeyConst& kc, const uint32_t* a, const
 cudaError_t launch_mul(int S, const KeyConst& kc, const uint32_t* a, const int64_t* k, uint32_t* out,
                        size_t count, uint32_t* scratch, int wm, uint32_t* err, int grid, unsigned long long* ctr,
                        cudaStream_t st);
+// Mul by multi-limb scalar magnitudes (el limbs each), window wb (1..8);
+// persistent grid of `grid` blocks (resident_blocks_mul_bn) with a scratch of
+// grid * instances_per_block(S, 0) * 2^(wb-1) * S limbs.
+cudaError_t launch_mul_bn(int S, const KeyConst& kc, const uint32_t* a, const uint32_t* emag, int el,
+                          uint32_t* out, size_t count, uint32_t* scratch, int wb, uint32_t* err, int grid,
+                          unsigned long long* ctr, cudaStream_t st);
+int resident_blocks_mul_bn(int S);
+// sel[i] = neg[i] ? -1 : 1 (selector of the batch inverse)
+cudaError_t launch_sel_from_neg(const uint8_t* neg, int64_t* sel, size_t count, cudaStream_t st);
 cudaError_t launch_decrypt(int Sp, const KeyConst& kc, const SecConst& sc, const uint32_t* ct, size_t count,
                            int64_t* out_i64, uint8_t* out_ovf, uint32_t* out_mag, uint8_t* out_neg,
                            uint32_t* scratch, uint32_t* err, int grid, unsigned long long* ctr, cudaStream_t st);
@@ -142,6 +151,9 @@ cudaError_t launch_matmul_planes(int S, const KeyConst& kc, const uint32_t* T, c
 cudaError_t launch_row_products(int S, const KeyConst& kc, const uint32_t* T, size_t rows, int K, uint32_t* prod,
                                 cudaStream_t st);
 cudaError_t launch_pow_shared(int S, const KeyConst& kc, uint32_t* v, size_t count, uint64_t e, cudaStream_t st);
+// the same for one exponent of el limbs in device memory (nonzero)
+cudaError_t launch_pow_shared_bn(int S, const KeyConst& kc, uint32_t* v, size_t count, const uint32_t* e, int el,
+                                 cudaStream_t st);
 cudaError_t launch_scale_rows(int S, const KeyConst& kc, uint32_t* out, const uint32_t* q, size_t r0, size_t rows,
                               int Ncols, cudaStream_t st);
 size_t subset_table_bytes_per_row(int S, int K);

@@ -209,6 +209,93 @@ __device__ __forceinline__ void mul_one(const KeyConst& kc, const uint32_t* __re
   if (active) store_slice<L>(out + i * S + g.t * L, acc);
 }
 
+// Mul(ct, k) for a scalar of any size up to `el` 32-bit limbs (magnitude in
+// `emag`, little-endian; the sign is applied afterwards by the batch
+// inverse).  evaluator.cc:99-123 takes any BigInt ("ciphertext overflow is
+// allowed"): c^|k| mod n^2 by left-to-right sliding windows of `wb` bits over
+// the limbs, odd powers c, c^3, .., c^(2^wb - 1) in this group's table `tb`.
+// |k| = 0 gives the Montgomery identity (evaluator.cc:105-106).
+template <int TPI, int L>
+__device__ __forceinline__ void mul_bn_one(const KeyConst& kc, const uint32_t* __restrict__ a,
+                                           const uint32_t* __restrict__ emag, int el, uint32_t* __restrict__ out,
+                                           size_t i, bool active, uint32_t* __restrict__ tb, int wb,
+                                           const uint32_t (&N)[L], const Group<TPI>& g, uint32_t* err) {
+  constexpr int S = TPI * L;
+  const int ntab = 1 << (wb - 1);
+  const uint32_t* e = emag + i * (size_t)el;
+  int pos = -1;
+#pragma unroll 1
+  for (int l = el - 1; l >= 0; --l) {
+    const uint32_t v = e[l];
+    if (v != 0u) {
+      pos = l * 32 + 31 - __clz(v);
+      break;
+    }
+  }
+  uint32_t x[L];
+  load_slice<L>(x, a + i * S + g.t * L);
+  check_ct<TPI, L>(x, N, active, g, err);
+  store_slice<L>(tb, x);
+  uint32_t x2[L], cur[L];
+  mont_mul<TPI, L>(x2, x, x, N, kc.np, g);
+  copy_slice<L>(cur, x);
+#pragma unroll 1
+  for (int t = 1; t < ntab; ++t) {
+    mont_mul<TPI, L>(cur, cur, x2, N, kc.np, g);
+    store_slice<L>(tb + (size_t)t * S, cur);
+  }
+  // the window ending at bit `top`: its lowest set bit j and its value
+  auto window = [&](int top, int& j) -> uint32_t {
+    j = max(top - wb + 1, 0);
+    while (!((e[j >> 5] >> (j & 31)) & 1u)) ++j;
+    return get_bits(e, el, j, top - j + 1);
+  };
+  uint32_t acc[L];
+  int sq = 0, mulidx = -1;
+  if (pos >= 0) {
+    int j;
+    const uint32_t val = window(pos, j);
+    load_slice<L>(acc, tb + (size_t)((val - 1) >> 1) * S);
+    pos = j - 1;
+  } else {
+    load_slice<L>(acc, kc.R1 + g.t * L);
+  }
+#pragma unroll 1
+  while (true) {
+    int op = 0;  // 0 = none, 1 = square, 2 = multiply by table[mulidx]
+    if (sq > 0) {
+      op = 1;
+      --sq;
+    } else if (mulidx >= 0) {
+      op = 2;
+    } else if (pos >= 0) {
+      if (!((e[pos >> 5] >> (pos & 31)) & 1u)) {
+        op = 1;
+        --pos;
+      } else {
+        int j;
+        const uint32_t val = window(pos, j);
+        sq = pos - j;
+        mulidx = (int)((val - 1) >> 1);
+        op = 1;
+        pos = j - 1;
+      }
+    }
+    if (!__any_sync(kFull, op != 0)) break;
+    uint32_t B[L];
+    if (op == 2) {
+      load_slice<L>(B, tb + (size_t)mulidx * S);
+      mulidx = -1;
+    } else {
+      copy_slice<L>(B, acc);
+    }
+    uint32_t res[L];
+    mont_mul<TPI, L>(res, acc, B, N, kc.np, g);
+    if (op != 0) copy_slice<L>(acc, res);
+  }
+  if (active) store_slice<L>(out + i * S + g.t * L, acc);
+}
+
 // ---------------------------------------------------------------------------
 // Decrypt (decryptor.cc:32-53): two groups per ciphertext, one per prime.
 //   x = REDC_p2(ct_mont) = c*Rp mod p^2;  y = x^(p-1) (sliding windows,

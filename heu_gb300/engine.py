@@ -288,7 +288,31 @@ class Key:
         return out
 
     def mul(self, a, k):
-        return self._ct_pt(self.lib.hg_mul, a, k)
+        """Mul(ct, k) (evaluator.cc:99-123).  k: int64 array, or Python ints of
+        any size up to the width of n^2 (then hg_mul_bn)."""
+        k_arr = np.asarray(k)
+        if k_arr.dtype != object and np.issubdtype(k_arr.dtype, np.integer) and k_arr.dtype.itemsize <= 8 and \
+                k_arr.dtype != np.uint64:
+            return self._ct_pt(self.lib.hg_mul, a, k_arr)
+        ks = [int(v) for v in k_arr.reshape(-1)]
+        if all(-(2 ** 63) <= v < 2 ** 63 for v in ks):
+            return self._ct_pt(self.lib.hg_mul, a, np.array(ks, dtype=np.int64))
+        return self.mul_bn(a, ks)
+
+    def mul_bn(self, a, ks):
+        a = self._ct(a)
+        ks = [int(v) for v in ks]
+        if a.shape[0] != len(ks):
+            raise ValueError("shape mismatch")
+        width = max(1, max((abs(v).bit_length() + 31) // 32 for v in ks) if ks else 1)
+        if width > self.ct_limbs:
+            raise ValueError("scalar wider than n^2")
+        mags = ints_to_limbs([abs(v) for v in ks], width)
+        neg = np.array([1 if v < 0 else 0 for v in ks], dtype=np.uint8)
+        out = self._out(a.shape[0])
+        capi.check(self.lib.hg_mul_bn(self.ctx.handle, self.id, _ptr(a), _ptr(mags), _ptr(neg), width, _ptr(out),
+                                      a.shape[0]))
+        return out
 
     def negate(self, a):
         a = self._ct(a)
@@ -362,14 +386,29 @@ class Key:
         return out
 
     def matmul(self, x, y):
-        """Ciphertext matrix x (M, K, S) times int64 matrix y (K, N) -> (M, N, S)."""
+        """Ciphertext matrix x (M, K, S) times integer matrix y (K, N) -> (M, N, S).
+        y: int64, or Python ints of any size up to the width of n^2 (then
+        hg_matmul_bn)."""
         x = np.ascontiguousarray(x, dtype=np.uint32)
-        y = np.ascontiguousarray(y, dtype=np.int64)
+        y = np.asarray(y)
         M, K = x.shape[0], x.shape[1]
-        if y.shape[0] != K:
+        if y.ndim != 2 or y.shape[0] != K:
             raise ValueError("dimension mismatch for matmul")
         N = y.shape[1]
         out = np.empty((M, N, self.ct_limbs), dtype=np.uint32)
+        if y.dtype == object or y.dtype == np.uint64:
+            vals = [int(v) for v in y.reshape(-1)]
+            if not all(-(2 ** 63) <= v < 2 ** 63 for v in vals):
+                width = max(1, max((abs(v).bit_length() + 31) // 32 for v in vals))
+                if width > self.ct_limbs:
+                    raise ValueError("plaintext wider than n^2")
+                mags = ints_to_limbs([abs(v) for v in vals], width)
+                neg = np.array([1 if v < 0 else 0 for v in vals], dtype=np.uint8)
+                capi.check(self.lib.hg_matmul_bn(self.ctx.handle, self.id, _ptr(x), M, K, _ptr(mags), _ptr(neg), width,
+                                                 N, _ptr(out)))
+                return out
+            y = np.array(vals, dtype=np.int64).reshape(K, N)
+        y = np.ascontiguousarray(y, dtype=np.int64)
         capi.check(self.lib.hg_matmul(self.ctx.handle, self.id, _ptr(x), M, K, _ptr(y), N, _ptr(out)))
         return out
 

@@ -42,6 +42,17 @@ def _as_values(values):
     return out.reshape(a.shape)
 
 
+
+def _matmul_plain(values):
+    """Plaintext operand of MatMul: int64 when every entry fits, else an
+    object array of Python ints (the engine then takes the multi-limb path)."""
+    v = np.asarray(values)
+    if v.dtype != object:
+        return np.asarray(v, dtype=np.int64)
+    if all(-(2 ** 63) <= int(e) < 2 ** 63 for e in v.reshape(-1)):
+        return np.array([int(e) for e in v.reshape(-1)], dtype=np.int64).reshape(v.shape)
+    return v
+
 class PlaintextArray:
     """Integer tensor (int64 or object dtype for values beyond int64)."""
 
@@ -548,7 +559,8 @@ class Evaluator:
         shape, ix, iy = _broadcast_index(x.shape, y.shape)
         p64, big = self._plain_i64(y, iy)
         if p64 is None:
-            raise ValueError("scalars must fit int64 for ciphertext multiplication")
+            # scalars of any size (evaluator.cc:99-123 takes any BigInt)
+            return CiphertextArray(self.kit, self.key.mul_bn(x.limbs[ix], [int(v) for v in big]), shape)
         return CiphertextArray(self.kit, self.key.mul(x.limbs[ix], p64), shape)
 
     def negate(self, x):
@@ -616,14 +628,14 @@ class Evaluator:
         (M, K) @ (K,) -> (M,))."""
         if isinstance(x, CiphertextArray) and isinstance(y, PlaintextArray):
             xv = x.grid() if x.ndim == 2 else x.grid().reshape(1, x.shape[0], -1)
-            yv = np.asarray(y.values, dtype=np.int64)
+            yv = _matmul_plain(y.values)
             yv = yv if yv.ndim == 2 else yv.reshape(-1, 1)
             out = self.key.matmul(xv, yv)
         elif isinstance(x, PlaintextArray) and isinstance(y, CiphertextArray):
             # (P @ C)^T = C^T @ P^T
             yv = y.grid() if y.ndim == 2 else y.grid().reshape(y.shape[0], 1, -1)
             ct_t = np.ascontiguousarray(np.transpose(yv, (1, 0, 2)))
-            pv = np.asarray(x.values, dtype=np.int64)
+            pv = _matmul_plain(x.values)
             pv = pv if pv.ndim == 2 else pv.reshape(1, -1)
             out = np.ascontiguousarray(np.transpose(self.key.matmul(ct_t, np.ascontiguousarray(pv.T)), (1, 0, 2)))
         else:

@@ -129,6 +129,13 @@ int hg_sub(hg_ctx* ctx, int key_id, const uint32_t* a, const uint32_t* b, uint32
 int hg_sub_plain(hg_ctx* ctx, int key_id, const uint32_t* a, const int64_t* p, uint32_t* out, size_t count);
 int hg_plain_sub(hg_ctx* ctx, int key_id, const int64_t* p, const uint32_t* a, uint32_t* out, size_t count);
 int hg_mul(hg_ctx* ctx, int key_id, const uint32_t* a, const int64_t* k, uint32_t* out, size_t count);
+/* Mul(ct, BigInt k) (paillier_zahlen/evaluator.cc:99-123, which takes a
+ * scalar of any size: "ciphertext overflow is allowed"): k[i] = (k_neg[i] ?
+ * -1 : 1) * the little-endian magnitude k_mag[i * k_limbs .. +k_limbs),
+ * 1 <= k_limbs <= S (scalars up to the width of n^2).  Same results as
+ * hg_mul where k fits int64. */
+int hg_mul_bn(hg_ctx* ctx, int key_id, const uint32_t* a, const uint32_t* k_mag, const uint8_t* k_neg,
+              size_t k_limbs, uint32_t* out, size_t count);
 int hg_negate(hg_ctx* ctx, int key_id, const uint32_t* a, uint32_t* out, size_t count);
 
 /* ---- heu.numpy reductions (numpy/evaluator.cc:355-373 Sum; the optional
@@ -151,6 +158,11 @@ int hg_bucket_sum(hg_ctx* ctx, int key_id, const uint32_t* x, size_t rows, size_
  * the vectorized Mul + ReduceSum path).  pt x ct is the transpose.        */
 int hg_matmul(hg_ctx* ctx, int key_id, const uint32_t* x, size_t M, size_t K, const int64_t* y, size_t N,
               uint32_t* out);
+/* MatMul with plaintexts of any size (numpy/evaluator.cc:208-353 takes any
+ * PMatrix): y(k,j) = (y_neg ? -1 : 1) * magnitude of y_limbs little-endian
+ * limbs at y_mag[(k * N + j) * y_limbs], 1 <= y_limbs <= S. */
+int hg_matmul_bn(hg_ctx* ctx, int key_id, const uint32_t* x, size_t M, size_t K, const uint32_t* y_mag,
+                 const uint8_t* y_neg, size_t y_limbs, size_t N, uint32_t* out);
 
 /* ---- representation ----------------------------------------------------- */
 int hg_to_mont(hg_ctx* ctx, int key_id, const uint32_t* z, uint32_t* mont, size_t count);
@@ -272,6 +284,8 @@ int hg_dev_add(hg_ctx* ctx, int key_id, const uint32_t* a, const uint32_t* b, ui
                void* stream);
 int hg_dev_mul(hg_ctx* ctx, int key_id, const uint32_t* a, const int64_t* k, uint32_t* out, size_t count,
                void* stream);
+int hg_dev_mul_bn(hg_ctx* ctx, int key_id, const uint32_t* a, const uint32_t* k_mag, const uint8_t* k_neg,
+                  size_t k_limbs, uint32_t* out, size_t count, void* stream);
 int hg_dev_sum(hg_ctx* ctx, int key_id, const uint32_t* a, size_t count, uint32_t* out, void* stream);
 /* EncryptZero / Randomize (encryptor.cc:26-33, evaluator.cc:25-28); ct is updated in place */
 int hg_dev_encrypt_zero(hg_ctx* ctx, int key_id, const uint32_t* r, uint32_t* ct_out, size_t count, void* stream);
@@ -307,6 +321,9 @@ int hg_dev_bucket_sum(hg_ctx* ctx, int key_id, const uint32_t* x, size_t rows, s
  * the host); x and out are device pointers. */
 int hg_dev_matmul(hg_ctx* ctx, int key_id, const uint32_t* x, size_t M, size_t K, const int64_t* y, size_t N,
                   uint32_t* out, void* stream);
+/* y_mag / y_neg stay in HOST memory, as for hg_dev_matmul. */
+int hg_dev_matmul_bn(hg_ctx* ctx, int key_id, const uint32_t* x, size_t M, size_t K, const uint32_t* y_mag,
+                     const uint8_t* y_neg, size_t y_limbs, size_t N, uint32_t* out, void* stream);
 int hg_dev_check(hg_ctx* ctx);
 
 /* ---- HEU wire format of ciphertext matrices ---------------------------------

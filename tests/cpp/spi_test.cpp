@@ -190,9 +190,14 @@ int main(int argc, char** argv) {
   EXPECT(dec.Decrypt(hea::ConstSpan<pg::Ciphertext>(std::vector<const pg::Ciphertext*>{&rs}))[0] ==
          a[0] + a[1] + a[2] + a[3]);
 
-  // errors: mismatched spans, scalar beyond int64, unpaired key
+  // scalars wider than int64 (evaluator.cc:99-123 takes any BigInt)
+  std::vector<pg::Plaintext> wide = {half, -half, pg::BigInt(1) - half, pg::BigInt::FromHex("10000000000000000")};
+  auto mul_big = ev.Mul(A, hea::ConstSpan<pg::Plaintext>(ptrs(wide)));
+  print_cts("mul_big", mul_big);
+
+  // errors: mismatched spans, scalar wider than n^2, unpaired key
   EXPECT(throws([&] { ev.Add(A, hea::ConstSpan<pg::Ciphertext>(ptrs(std::vector<pg::Ciphertext>(ca.begin(), ca.begin() + 2)))); }));
-  std::vector<pg::Plaintext> huge = {half};
+  std::vector<pg::Plaintext> huge = {pg::BigInt::FromMag(pk.n_square_.Mag() * pk.n_square_.Mag(), false)};
   EXPECT(throws([&] { ev.Mul(hea::ConstSpan<pg::Ciphertext>(std::vector<const pg::Ciphertext*>{&ca[0]}),
                              hea::ConstSpan<pg::Plaintext>(ptrs(huge))); }));
   pg::SecretKey sk2;

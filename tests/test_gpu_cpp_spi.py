@@ -45,4 +45,7 @@ def test_cpp_spi_matches_oracle(bits):
         assert int(got[f"mul_cp[{i}]"], 16) == mont(pz.mul(pk, ca[i], b[i]))
         assert int(got[f"neg[{i}]"], 16) == mont(pz.negate(pk, ca[i]))
     assert int(got["sum"], 16) == mont(pz.sum_(pk, ca))
+    wide = [half, -half, 1 - half, 2 ** 64]
+    for i, kv in enumerate(wide):
+        assert int(got[f"mul_big[{i}]"], 16) == mont(pz.mul(pk, ca[i], kv)), f"mul_big[{i}]"
     assert pz.decrypt(pk, sk, pz.from_mont(pk, int(got["sum"], 16))) == sum(a)

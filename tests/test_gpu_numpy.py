@@ -102,6 +102,24 @@ def test_matmul_signed_and_extreme_scalars(gpu_key):
     assert zform(key, out) == [v for row in pz.matmul(pk, cx, yb.tolist()) for v in row]
 
 
+def test_matmul_bigint_plaintexts(gpu_key):
+    """MatMul with plaintext entries wider than int64 (numpy/evaluator.cc:
+    208-353 takes any PMatrix), including negative ones and n/2."""
+    key, pk, sk = gpu_key(2048, 0)
+    rng = np.random.default_rng(10)
+    x = rng.integers(-(2 ** 20), 2 ** 20, size=(2, 5))
+    ct, zs = enc_matrix(key, pk, x, 56)
+    y = np.array([[2 ** 70, -(2 ** 100), 3], [0, pk.n // 2, -1], [-(pk.n // 2), 5, 2 ** 64],
+                  [1, -(2 ** 63), 2 ** 63], [-(2 ** 65) + 3, 7, 0]], dtype=object)
+    out = key.matmul(ct.reshape(2, 5, -1), y)
+    cx = [[zs[i * 5 + j] for j in range(5)] for i in range(2)]
+    assert zform(key, out) == [v for row in pz.matmul(pk, cx, y.tolist()) for v in row]
+    # non-negative wide entries take no offset
+    yp = np.array([[2 ** 80 + i * j for j in range(3)] for i in range(5)], dtype=object)
+    out = key.matmul(ct.reshape(2, 5, -1), yp)
+    assert zform(key, out) == [v for row in pz.matmul(pk, cx, yp.tolist()) for v in row]
+
+
 def test_config3_bucket_sum_full_size(gpu_key):
     """2^20 fixed-point gradients (scale 2^20), 64 features x 256 buckets:
     decrypted bucket sums equal the integer bucket sums."""

@@ -184,6 +184,60 @@ def test_mul_all_positive_skips_inverse(kk):
     assert_ct_equal(pk, key, out, [pz.mul(pk, z, k) for z, k in zip(zs, ks)], "mul positive")
 
 
+def test_mul_bigint_scalars(kk):
+    """Mul(ct, BigInt) (evaluator.cc:99-123): scalars wider than int64, up to
+    the width of n^2, byte-equal to the oracle; int64-range values through the
+    multi-limb path equal hg_mul's."""
+    key, pk, sk = kk
+    half = pk.n // 2
+    ks = [2 ** 64, -(2 ** 64), 2 ** 200 + 12345, -(2 ** 200), half, -half, half - 1, pk.n, pk.n2 - 1,
+          -(pk.n2 - 1), 2 ** 63, -(2 ** 63) - 1, 0, 1, -1, 7]
+    prg = Prg(19)
+    ks += [prg.below(pk.n) - pk.n // 2 for _ in range(16)]
+    n = len(ks)
+    ms = rand_i64(prg, n, -(2 ** 31), 2 ** 31)
+    zs = [pz.encrypt(pk, m, r) for m, r in zip(ms, pz.r_stream(26, n, pk.key_size // 2))]
+    c = to_mont_limbs(pk, key, zs)
+    out = key.mul(c, np.array(ks, dtype=object))
+    assert_ct_equal(pk, key, out, [pz.mul(pk, z, k) for z, k in zip(zs, ks)], "mul bigint")
+    small = [0, 1, -1, 2, -3, I64_MAX, I64_MIN + 1, 2 ** 40]
+    assert np.array_equal(key.mul_bn(c[:8], small), key.mul(c[:8], np.array(small, dtype=np.int64)))
+    # decryptions: m * k mod n, centred
+    dm = key.decrypt_bn(out[:6])
+    for got, m, k in zip(dm, ms, ks):
+        want = (m * k) % pk.n
+        assert got == (want - pk.n if want > pk.n // 2 else want)
+
+
+def test_mul_bigint_device_form_and_limits(kk):
+    torch = pytest.importorskip("torch")
+    import ctypes
+
+    key, pk, sk = kk
+    ks = [2 ** 100 + 1, -(2 ** 90), 5, 0, -(pk.n // 2)]
+    zs = [pz.encrypt(pk, m, r) for m, r in zip([3, -4, 5, 6, 7], pz.r_stream(27, 5, pk.key_size // 2))]
+    c = to_mont_limbs(pk, key, zs)
+    width = key.ct_limbs // 2
+    mags = hg.ints_to_limbs([abs(k) for k in ks], width)
+    neg = np.array([k < 0 for k in ks], dtype=np.uint8)
+    P = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+    dc = torch.from_numpy(c.view(np.int32)).cuda()
+    dm = torch.from_numpy(mags.view(np.int32)).cuda()
+    dn = torch.from_numpy(neg).cuda()
+    dout = torch.zeros_like(dc)
+    capi.check(key.lib.hg_dev_mul_bn(key.ctx.handle, key.id, P(dc), P(dm), P(dn), width, P(dout), 5, None))
+    torch.cuda.synchronize()
+    capi.check(key.lib.hg_dev_check(key.ctx.handle))
+    got = dout.cpu().numpy().view(np.uint32)
+    assert_ct_equal(pk, key, got, [pz.mul(pk, z, k) for z, k in zip(zs, ks)], "dev mul bigint")
+    # scalars wider than n^2 are rejected before any work
+    too = hg.ints_to_limbs([1], key.ct_limbs + 1)
+    out = np.zeros_like(c[:1])
+    rc = key.lib.hg_mul_bn(key.ctx.handle, key.id, hg.engine._ptr(c[:1]), hg.engine._ptr(too),
+                           hg.engine._ptr(np.zeros(1, np.uint8)), key.ct_limbs + 1, hg.engine._ptr(out), 1)
+    assert rc == capi.HG_ERR_INVALID
+
+
 @pytest.mark.parametrize("count", [1, 2, 3, 17, 255, 256, 257, 900])
 def test_sum_counts(gpu_key, count):
     key, pk, sk = gpu_key(2048, 0)
@@ -206,6 +260,34 @@ def test_ciphertext_range_rejected(kk):
         with pytest.raises(hg.HgError) as ei:
             fn()
         assert ei.value.code == capi.HG_ERR_CT_RANGE
+
+
+def test_sum_checks_every_input(gpu_key):
+    """A value >= n^2 anywhere in a Sum input is rejected (evaluator.cc:21-23
+    VALIDATE), not only at the first element of a reduction chunk."""
+    key, pk, sk = gpu_key(2048, 0)
+    good = pz.to_mont(pk, pz.encrypt(pk, 7, 3))
+    for n, bad_at in ((2, 1), (64, 63), (300_000, 12_345), (300_000, 299_999)):
+        zs = np.tile(hg.ints_to_limbs([good], key.ct_limbs), (n, 1))
+        zs[bad_at] = hg.ints_to_limbs([pk.n2 + 1], key.ct_limbs)[0]
+        with pytest.raises(hg.HgError) as ei:
+            key.sum(zs)
+        assert ei.value.code == capi.HG_ERR_CT_RANGE, (n, bad_at)
+    # the device-pointer form reports the same
+    torch = pytest.importorskip("torch")
+    import ctypes
+
+    zs = np.tile(hg.ints_to_limbs([good], key.ct_limbs), (64, 1))
+    zs[63] = hg.ints_to_limbs([pk.n2], key.ct_limbs)[0]
+    d = torch.from_numpy(zs.view(np.int32)).cuda()
+    out = torch.zeros((1, key.ct_limbs), dtype=torch.int32, device="cuda")
+    capi.check(key.lib.hg_dev_sum(key.ctx.handle, key.id, ctypes.c_void_p(d.data_ptr()), 64,
+                                  ctypes.c_void_p(out.data_ptr()), None))
+    torch.cuda.synchronize()
+    assert key.lib.hg_dev_check(key.ctx.handle) == capi.HG_ERR_CT_RANGE
+    # and a valid input still sums after the error
+    zs[63] = zs[0]
+    assert hg.limbs_to_ints(key.from_mont(key.sum(zs))) == [pz.sum_(pk, [pz.encrypt(pk, 7, 3)] * 64)]
 
 
 def test_montgomery_conversion_roundtrip(kk):
