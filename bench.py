@@ -150,8 +150,26 @@ def cpu_sample(seconds_hint=10.0, threads=None):
     rates["decrypt"] = n_dec / (time.perf_counter() - t)
     assert np.array_equal(d, (m + m[::-1])[:n_dec]), "CPU baseline decrypt mismatch"
     step_rate = 4.0 / sum(1.0 / rates[o] for o in ("encrypt", "add", "mul", "decrypt"))
+    # reductions (numpy/evaluator.cc:208-458) on the same ciphertexts
+    ctc = np.ascontiguousarray(ct)
+    t = time.perf_counter()
+    for _ in range(4):
+        ck.sum_mt(ctc, threads)
+    rates["sum"] = 4 * n_fast / (time.perf_counter() - t)
+    nb_rows, F, B = min(n_fast, 4096), 64, 256
+    om = rng.integers(0, B, size=(nb_rows, F)).astype(np.uint8)
+    t = time.perf_counter()
+    ck.bucket_sum(ctc[:nb_rows], om, B, threads)
+    rates["bucket_sum_row_features"] = nb_rows * F / (time.perf_counter() - t)
+    Mm, K, N = 1, 256, 32
+    y = rng.integers(-(2 ** 15), 2 ** 15, size=(K, N), dtype=np.int64)
+    t = time.perf_counter()
+    ck.matmul(ctc[: Mm * K].reshape(Mm, K, -1), y, threads)
+    rates["matmul_outputs"] = Mm * N / (time.perf_counter() - t)
     sample = (f"{n_fast} encrypt+add, {n_mul} mul (64-bit k), {n_dec} CRT decrypt on 2048-bit key; "
-              "step-equivalent rate = 4/(sum 1/rate_op)")
+              "step-equivalent rate = 4/(sum 1/rate_op); reductions: Sum of {0} x4, bucket-sum {1} rows x 64 "
+              "features x 256 buckets, MatMul {2}x256 @ 256x32 int32 (per-element Mul + reduce as "
+              "numpy/evaluator.cc)".format(n_fast, nb_rows, Mm))
     return rates, step_rate, threads, sample
 
 
@@ -529,6 +547,16 @@ def ours_arm(args):
         cpu = {"value": step_rate, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample,
                "per_op": rates}
 
+    extras = {}
+    if rank == 0 and world == 1 and not args.no_extras:
+        # the rest of the metric, outside the timed step: reductions (config 3),
+        # the uneven batch against plain calls (config 4), the served stream at
+        # a sub-capacity and a saturating rate (config 5); each in its own
+        # context once this one has released its table
+        ctx.close()
+        ctx = None
+        extras = run_extras(args)
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -555,12 +583,36 @@ def ours_arm(args):
             "gpu_launches": launches,
             "clocks": clocks,
         }
+        line.update(extras)
+        if "reductions" in extras:
+            per_op["sum"] = extras["reductions"]["sum"]["units_per_s"]
         print(json.dumps(line), flush=True)
     if dist:
         dist.barrier()
         dist.destroy_process_group()
-    ctx.close()
+    if ctx is not None:
+        ctx.close()
     return 0
+
+
+def run_extras(args):
+    """Summaries of configs 3, 4 and 5 for the default line (each measured
+    with CUDA events or wall clocks in its own context, after the main step's
+    timed region)."""
+    out = {}
+    c3 = c3_measure(args, 2, 1)
+    out["reductions"] = {k: {"seconds": v["seconds"], "units_per_s": v["units_per_s"],
+                             "algorithmic_tmacs": v["algorithmic_tmacs"], "hbm_gbs": v["hbm_gbs"]}
+                         for k, v in c3["results"].items()}
+    out["reductions"]["config"] = c3["config"]
+    c4 = c4_measure(args, 2, 1)
+    out["batched_vs_plain"] = {"batched_over_plain": c4["batched_over_plain"],
+                               "batched_ops_per_s": c4["value"], "plain_ops_per_s": c4["plain_per_call_ops_per_s"],
+                               "steps": c4["steps"], "config": c4["config"]}
+    c5 = c5_measure(args, [50, 3000], lambda rate: 250 if rate <= 100 else 1000)
+    out["serve"] = {"served_over_plain": c5["served_over_plain"], "plain_ops_per_s": c5["plain_per_call_ops_per_s"],
+                    "rates": c5["rates"], "config": c5["config"]}
+    return out
 
 
 # ---------------------------------------------------------------------------
@@ -584,6 +636,11 @@ def c4_arm(args):
     log-uniform in [16, 262144], op mix 40% encrypt / 30% mul / 20% add / 10%
     decrypt, int64 plaintexts and scalars uniform), run as one persistent
     launch replayed from a CUDA graph, against the plain per-call kernels."""
+    print(json.dumps(c4_measure(args, args.steps, args.warmup)), flush=True)
+    return 0
+
+
+def c4_measure(args, steps, warmup):
     import numpy as np
     import torch
 
@@ -680,14 +737,14 @@ def c4_arm(args):
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) / 1e3
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         plain()
         batch.run(stream=stream, graph=True)
     batch.wait(stream=stream)
     capi.check(lib.hg_dev_check(h))
-    t_plain = timed(plain, args.steps)
+    t_plain = timed(plain, steps)
     launches0 = capi.launch_count()
-    t_batch = timed(lambda: batch.run(stream=stream, graph=True), args.steps)
+    t_batch = timed(lambda: batch.run(stream=stream, graph=True), steps)
     launches = capi.launch_count() - launches0
     batch.wait(stream=stream)
     capi.check(lib.hg_dev_check(h))
@@ -701,19 +758,18 @@ def c4_arm(args):
         mix[f"{nm}_{j['key'].key_bits}"] = mix.get(f"{nm}_{j['key'].key_bits}", 0) + j["n"]
     line = {
         "metric": "Paillier ops/s, 64 uneven jobs over 1024/2048/3072-bit keys (config 4), batched vs plain GPU",
-        "value": total * args.steps / t_batch, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": t_batch / args.steps * 1e3, "higher_is_better": True,
+        "value": total * steps / t_batch, "unit": UNIT, "n_gpus": 1, "steps": steps,
+        "warmup": warmup, "ms_per_step": t_batch / steps * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
         "config": {"workload": "config4", "jobs": 64, "elements_per_step": total, "mix": mix,
                    "batch_variant": best_v, "graph": True},
-        "plain_per_call_ops_per_s": total * args.steps / t_plain,
+        "plain_per_call_ops_per_s": total * steps / t_plain,
         "batched_over_plain": t_plain / t_batch,
         "gpu_launches": launches,
     }
-    print(json.dumps(line), flush=True)
     batch.close()
     ctx.close()
-    return 0
+    return line
 
 
 def c3_arm(args):
@@ -721,6 +777,11 @@ def c3_arm(args):
     gradients (N(0,1) * 2^20): Sum of 2^20 ciphertexts, FeatureWiseBucketSum
     over 64 features x 256 buckets, MatMul 4096x256 ciphertexts @ 256x64
     int32 in [-2^15, 2^15)."""
+    print(json.dumps(c3_measure(args, args.steps, args.warmup)), flush=True)
+    return 0
+
+
+def c3_measure(args, steps, warmup):
     import numpy as np
     import torch
 
@@ -766,18 +827,18 @@ def c3_arm(args):
             ("sum", run_sum, n, mm_macs(128), n * cb + cb),
             ("bucket_sum", run_bucket, n * F, mm_macs(128), n * cb + n * F + F * B * cb),
             ("matmul", run_matmul, M * N, (K + 16) * mm_macs(128), M * K * cb + K * N * 8 + M * N * cb)):
-        for _ in range(max(1, args.warmup)):
+        for _ in range(max(1, warmup)):
             fn()
         torch.cuda.synchronize()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         with torch.cuda.stream(stream):
             e0.record(stream)
-            for _ in range(args.steps):
+            for _ in range(steps):
                 fn()
             e1.record(stream)
         torch.cuda.synchronize()
-        dt = e0.elapsed_time(e1) / 1e3 / args.steps
+        dt = e0.elapsed_time(e1) / 1e3 / steps
         res[name] = {"seconds": dt, "units_per_s": units / dt, "algorithmic_tmacs": units * macs_per_unit / dt / 1e12,
                      "algorithmic_bytes": nbytes, "hbm_gbs": nbytes / dt / 1e9}
     capi.check(lib.hg_dev_check(h))
@@ -797,14 +858,13 @@ def c3_arm(args):
     line = {
         "metric": "heu.numpy reductions on 2048-bit ciphertexts (config 3): Sum, bucket-sum, MatMul",
         "value": res["bucket_sum"]["units_per_s"], "unit": "ciphertext-products/s (bucket-sum)",
-        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+        "n_gpus": 1, "steps": steps, "warmup": warmup, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u32", "data": "synthetic",
         "config": {"workload": "config3", "sum_n": n, "bucket_sum": [n, F, B], "matmul": [M, K, N]},
         "results": res, "mac_peak_tmacs": peak,
     }
-    print(json.dumps(line), flush=True)
     ctx.close()
-    return 0
+    return line
 
 
 def ou_arm(args):
@@ -1071,6 +1131,38 @@ def c5_arm(args):
     [1, 65536], op mix encrypt/add/mul/sum/decrypt 30/20/25/15/10, resident
     ciphertext vectors, 40 GB device budget; p50/p99 latency and throughput
     per rate, against the same mix through plain per-call kernels."""
+    rates = [20, 50, 100, 300, 1000, 3000, 10000, 50000] if not args.quick else [50, 3000]
+    if args.rates:
+        rates = [int(v) for v in args.rates.split(",")]
+    print(json.dumps(c5_measure(args, rates, lambda rate: min(1000, max(200, int(rate * 3))))), flush=True)
+    return 0
+
+
+OP_NAMES = ("encrypt", "decrypt", "add", "mul", "sum")
+
+
+def _latency_classes(lat, ops, lens, short_len):
+    """p50/p99 (ms) by class: all, short (<= short_len elements) split into
+    decrypt and the other ops, per op among the short ones, and long."""
+    import numpy as np
+
+    def pct(mask):
+        if not mask.any():
+            return None
+        v = lat[mask] * 1e3
+        return {"requests": int(mask.sum()), "p50_ms": float(np.percentile(v, 50)),
+                "p99_ms": float(np.percentile(v, 99)), "max_ms": float(v.max())}
+
+    short = lens <= short_len
+    out = {"short_le_%d" % short_len: pct(short),
+           "short_non_decrypt": pct(short & (ops != 1)),
+           "short_decrypt": pct(short & (ops == 1)),
+           "long": pct(~short)}
+    out["short_by_op"] = {OP_NAMES[o]: pct(short & (ops == o)) for o in range(5)}
+    return out
+
+
+def c5_measure(args, rates, nreq_for_rate):
     import numpy as np
     import torch
 
@@ -1098,7 +1190,7 @@ def c5_arm(args):
 
     server = hg.Server(ctx, budget_bytes=40 << 30, slots=args.slots, max_batch_elems=1 << 18,
                        batch_us=args.batch_us, slice_us=args.slice_us, policy=args.policy,
-                       express_us=args.express_us)
+                       express_us=args.express_us, express_len=args.express_len)
     for key in keys:
         m = torch.randint(-(2 ** 40), 2 ** 40, (LMAX,), dtype=torch.int64, device=dev, generator=gen)
         r = torch.randint(-(2 ** 31), 2 ** 31, (LMAX, key.r_limbs), dtype=torch.int32, device=dev, generator=gen)
@@ -1115,14 +1207,11 @@ def c5_arm(args):
     key_ids = (ctypes.c_int * len(keys))(*[k.id for k in keys])
     hnd = (ctypes.c_uint64 * len(keys))(*handles)
     weights = [0.30, 0.20, 0.25, 0.15, 0.10]  # encrypt, add, mul, sum, decrypt
-    rates = [100, 300, 1000, 3000, 10000, 50000] if not args.quick else [300, 3000]
-    if args.rates:
-        rates = [int(v) for v in args.rates.split(",")]
     results = []
     # warm-up: a short stream
     for rate, nreq, seed in [(1000, 50, 1)] + [(rt, 0, 0) for rt in rates]:
         if nreq == 0:
-            nreq = min(1000, max(200, int(rate * 3)))
+            nreq = nreq_for_rate(rate)
             seed = int(rate)
         ls = capi.LoadSpec()
         ls.key_ids = ctypes.cast(key_ids, ctypes.c_void_p)
@@ -1147,13 +1236,12 @@ def c5_arm(args):
         if seed == 1:
             continue
         nb = server.stats()["batches"] - b0
-        short = lens <= 1024
+        offered = rate * (LMAX - 1) / np.log(LMAX)  # mean of the log-uniform length times the rate
         results.append({"rate_req_per_s": rate, "requests": nreq,
+                        "offered_elems_per_s": float(offered),
                         "p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
                         "mean_ms": float(lat.mean() * 1e3),
-                        "short_le_1024": {"requests": int(short.sum()),
-                                          "p50_ms": float(np.percentile(lat[short], 50) * 1e3) if short.any() else None,
-                                          "p99_ms": float(np.percentile(lat[short], 99) * 1e3) if short.any() else None},
+                        "classes": _latency_classes(lat, ops, lens, 1024),
                         "throughput_req_per_s": nreq / wall.value,
                         "throughput_ops_per_s": float(lens.sum()) / wall.value,
                         "micro_batches": int(nb), "wall_s": wall.value})
@@ -1205,15 +1293,18 @@ def c5_arm(args):
                    "budget_bytes": 40 << 30, "slots": args.slots, "max_batch_elems": 1 << 18,
                    "batch_us": args.batch_us or 100000.0, "slice_us": args.slice_us or 50000.0,
                    "policy": ["shortest-remaining-first", "fifo"][args.policy],
-                   "express_us": args.express_us if args.express_us > 0 else None},
+                   "express_us": args.express_us if args.express_us > 0 else None,
+                   "express_len": args.express_len or None,
+                   "capacity_note": "mean request = (65536-1)/ln(65536) = 5,909 elements, so rates above "
+                                    "~200 req/s offer more elements/s than one GB300 serves; lower rates are "
+                                    "sub-capacity"},
         "rates": results,
         "plain_per_call_ops_per_s": plain_ops,
         "served_over_plain": peak_served / plain_ops,
     }
-    print(json.dumps(line), flush=True)
     server.close()
     ctx.close()
-    return 0
+    return line
 
 
 def main():
@@ -1237,7 +1328,11 @@ def main():
     ap.add_argument("--quick", action="store_true", help="config5: two arrival rates only")
     ap.add_argument("--batch-us", type=float, default=0.0, help="config5: server micro-batch target (0 = default)")
     ap.add_argument("--slice-us", type=float, default=0.0, help="config5: server slice per request (0 = default)")
-    ap.add_argument("--slots", type=int, default=4, help="config5: concurrent micro-batches")
+    ap.add_argument("--slots", type=int, default=5, help="config5: concurrent micro-batches")
+    ap.add_argument("--express-len", type=int, default=1024,
+                    help="config5: requests of at most this many elements run in the latency class (0 = off)")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="default workload: skip the reductions, batched and served summaries")
     ap.add_argument("--policy", type=int, default=0, choices=[0, 1], help="config5: 0 shortest-first, 1 fifo")
     ap.add_argument("--rates", default="", help="config5: comma-separated arrival rates (req/s)")
     ap.add_argument("--express-us", type=float, default=0.0,

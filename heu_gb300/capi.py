@@ -127,7 +127,8 @@ class ServerConfig(ctypes.Structure):
 
     _fields_ = [("budget_bytes", ctypes.c_size_t), ("slots", ctypes.c_int), ("max_batch_elems", ctypes.c_size_t),
                 ("variant", ctypes.c_int), ("batch_us", ctypes.c_double), ("slice_us", ctypes.c_double),
-                ("policy", ctypes.c_int), ("express_us", ctypes.c_double), ("express_share", ctypes.c_double)]
+                ("policy", ctypes.c_int), ("express_us", ctypes.c_double), ("express_share", ctypes.c_double),
+                ("express_len", ctypes.c_size_t)]
 
 
 class Request(ctypes.Structure):

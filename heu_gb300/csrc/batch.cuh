@@ -33,13 +33,16 @@ struct BatchTile {
 };
 
 // (threads per instance) for n^2 with S limbs and (threads per side) for p^2
-// with SP limbs, per variant; must match HG_DISPATCH_SV / HG_DISPATCH_SPV.
+// with SP limbs, per variant; V = 0 / 1 must match HG_DISPATCH_SV /
+// HG_DISPATCH_SPV, V = 2 (latency layout) HG_DISPATCH_SL / HG_DISPATCH_SPL.
 __host__ __device__ constexpr int tpi_for(int S, int V) {
-  return S == 64 ? (V ? 8 : 4) : S == 128 ? (V ? 4 : 8) : (V ? 8 : 16);
+  return V == 2 ? 32 : S == 64 ? (V ? 8 : 4) : S == 128 ? (V ? 4 : 8) : (V ? 8 : 16);
 }
 __host__ __device__ constexpr int tp_for(int SP, int V) {
-  return SP == 32 ? (V ? 4 : 2) : SP == 64 ? (V ? 8 : 4) : (V ? 4 : 8);
+  return V == 2 ? 16 : SP == 32 ? (V ? 4 : 2) : SP == 64 ? (V ? 8 : 4) : (V ? 4 : 8);
 }
+// Variant set of the latency layout (short requests).
+constexpr int kBatchLatencyVariant = 2;
 
 int batch_resident_blocks(int variant);
 int batch_warps_per_block();

@@ -62,12 +62,38 @@ int resident_blocks_decrypt(int Sp, int variant) {
   return r;
 }
 
+// Ciphertexts of one wave of the latency layout (a half warp per CRT side,
+// one ciphertext per warp); batches up to this size run in that layout.
+static size_t latency_wave_decrypt(int Sp) {
+  static size_t cache[3] = {0, 0, 0};
+  const int slot = Sp == 32 ? 0 : Sp == 64 ? 1 : 2;
+  if (cache[slot] == 0) {
+    size_t v = 0;
+    [&]() -> cudaError_t {
+      HG_DISPATCH_SPL(Sp, v = (size_t)occupancy_blocks(k_decrypt<TP, LP>) * (kBlock / 32));
+      return cudaSuccess;
+    }();
+    cache[slot] = v;
+  }
+  return cache[slot];
+}
+
 cudaError_t launch_decrypt(int Sp, const KeyConst& kc, const SecConst& sc, const uint32_t* ct, size_t count,
                            int64_t* out_i64, uint8_t* out_ovf, uint32_t* out_mag, uint8_t* out_neg,
                            uint32_t* scratch, uint32_t* err, int grid, unsigned long long* ctr, cudaStream_t st) {
   if (count == 0) return cudaSuccess;
   const cudaError_t e = cudaMemsetAsync(ctr, 0, sizeof(*ctr), st);
   if (e != cudaSuccess) return e;
+  // the latency layout's unit slots must fit the scratch sized for `grid`
+  // blocks of the throughput layout
+  const size_t lat_blocks = (count + kBlock / 32 - 1) / (kBlock / 32);
+  if (count <= latency_wave_decrypt(Sp) &&
+      lat_blocks * (kBlock / 32) <= (size_t)grid * units_per_block_decrypt(Sp, sc.variant)) {
+    HG_DISPATCH_SPL(Sp, k_decrypt<TP, LP><<<(unsigned)lat_blocks, kBlock, 0, st>>>(
+                            kc, sc, ct, count, out_i64, out_ovf, out_mag, out_neg, scratch, err, ctr));
+    count_launches(1);
+    return cudaGetLastError();
+  }
   HG_DISPATCH_SPV(Sp, sc.variant, {
     const size_t upb = kBlock / (2 * TP);
     const unsigned need = (unsigned)((count + upb - 1) / upb);

@@ -2548,9 +2548,14 @@ int hg_server_create(hg_ctx* ctx, const hg_server_config* cfg, hg_server** out) 
     const int bps = hg::batch_blocks_per_sm(c.variant);
     const int sms = std::max(1, resident / std::max(1, bps));
     s->express_us = (cfg && cfg->express_us != 0.0) ? cfg->express_us : -1.0;
+    s->express_len = cfg ? cfg->express_len : 0;
+    if (s->express_len > 0) s->express_us = 0.0;  // the length rule replaces the cost rule
     const double share = (cfg && cfg->express_share > 0.0) ? cfg->express_share : 0.25;
     if (share >= 1.0) fail(HG_ERR_INVALID, "express_share must be below 1");
-    if (c.slots < 2 || bps < 2) s->express_us = -1.0;
+    if (c.slots < 2 || bps < 2) {
+      s->express_us = -1.0;
+      s->express_len = 0;
+    }
     s->regular_grid = resident;
     if (s->express_us >= 0.0) {
       // express: `eb` blocks on every SM; regular batches: the rest
@@ -2577,6 +2582,9 @@ int hg_server_create(hg_ctx* ctx, const hg_server_config* cfg, hg_server** out) 
     for (int i = 0; i < c.slots; ++i) {
       auto sl = std::make_unique<Slot>();
       sl->express = (i == 0 && s->express_us >= 0.0);
+      // a second express slot for short decryptions (latency class by length)
+      sl->express_dec = (i == 1 && s->express_len > 0 && c.slots >= 3);
+      if (sl->express_dec) sl->express = true;
       int lo_prio = 0, hi_prio = 0;
       cuda_check(cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio), "priority range");
       cuda_check(cudaStreamCreateWithPriority(&sl->st, cudaStreamNonBlocking, sl->express ? hi_prio : lo_prio),

@@ -305,6 +305,37 @@ int instances_per_block(int S, int variant) {
   return kBlock / tpi;
 }
 
+// Instances of one wave of a latency-layout kernel (one instance per warp):
+// batches up to this size run in that layout, since they leave the GPU
+// mostly idle in the throughput layout and finish sooner with fewer limbs
+// per lane on each dependent chain.
+template <typename K>
+static size_t latency_wave(K kernel) {
+  return (size_t)occupancy_blocks(kernel) * (kBlock / 32);
+}
+
+static size_t latency_wave_encrypt(int S) {
+  static size_t cache[3] = {0, 0, 0};
+  const int slot = S == 64 ? 0 : S == 128 ? 1 : 2;
+  if (cache[slot] == 0) {
+    size_t v = 0;
+    [&]() -> cudaError_t { HG_DISPATCH_SL(S, v = latency_wave(k_encrypt<TPI, L>)); return cudaSuccess; }();
+    cache[slot] = v;
+  }
+  return cache[slot];
+}
+
+static size_t latency_wave_mul(int S) {
+  static size_t cache[3] = {0, 0, 0};
+  const int slot = S == 64 ? 0 : S == 128 ? 1 : 2;
+  if (cache[slot] == 0) {
+    size_t v = 0;
+    [&]() -> cudaError_t { HG_DISPATCH_SL(S, v = latency_wave(k_mul<TPI, L>)); return cudaSuccess; }();
+    cache[slot] = v;
+  }
+  return cache[slot];
+}
+
 int resident_blocks_mul(int S, int variant) {
   int r = 0;
   [&]() -> cudaError_t { HG_DISPATCH_SV(S, variant, r = occupancy_blocks(k_mul<TPI, L>)); return cudaSuccess; }();
@@ -316,6 +347,11 @@ cudaError_t launch_encrypt(int S, const KeyConst& kc, EncMode mode, const int64_
                            size_t count, uint32_t* err, int grid, cudaStream_t st) {
   (void)grid;
   if (count == 0) return cudaSuccess;
+  if (count <= latency_wave_encrypt(S)) {
+    HG_DISPATCH_SL(S, k_encrypt<TPI, L><<<blocks_for(count, TPI), kBlock, 0, st>>>(kc, mode, m, m_mag, m_neg, r,
+                                                                                  ct_in, out, count, err));
+    return counted();
+  }
   HG_DISPATCH_SV(S, kc.variant,
                  k_encrypt<TPI, L><<<blocks_for(count, TPI), kBlock, 0, st>>>(kc, mode, m, m_mag, m_neg, r, ct_in,
                                                                              out, count, err));
@@ -344,6 +380,15 @@ cudaError_t launch_mul(int S, const KeyConst& kc, const uint32_t* a, const int64
   if (count == 0) return cudaSuccess;
   const cudaError_t e = cudaMemsetAsync(ctr, 0, sizeof(*ctr), st);
   if (e != cudaSuccess) return e;
+  // the latency layout's instance slots must fit the scratch sized for
+  // `grid` blocks of the throughput layout
+  const size_t lat_blocks = blocks_for(count, 32);
+  if (count <= latency_wave_mul(S) &&
+      lat_blocks * (kBlock / 32) <= (size_t)grid * instances_per_block(S, kc.variant)) {
+    HG_DISPATCH_SL(S, k_mul<TPI, L><<<(unsigned)lat_blocks, kBlock, 0, st>>>(kc, a, k, out, count, scratch, wm, err,
+                                                                            ctr));
+    return counted();
+  }
   HG_DISPATCH_SV(S, kc.variant, {
     const unsigned need = blocks_for(count, TPI);
     const unsigned gb = (unsigned)std::min((size_t)need, (size_t)grid);

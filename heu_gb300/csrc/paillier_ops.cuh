@@ -609,3 +609,22 @@ __device__ __forceinline__ size_t next_work(unsigned long long* ctr, int per_war
     case 193: { constexpr int TP = 4, LP = 24; __VA_ARGS__; } break;                     \
     default: return cudaErrorInvalidValue;                                               \
   }
+
+// Latency layout (short batches): a whole warp per instance mod n^2 and a
+// half warp per CRT side mod p^2, so each dependent chain of Montgomery
+// multiplications advances with 2-6 limbs per lane instead of 8-24.
+#define HG_DISPATCH_SL(S, ...)                                                           \
+  switch (S) {                                                                           \
+    case 64: { constexpr int TPI = 32, L = 2; __VA_ARGS__; } break;                      \
+    case 128: { constexpr int TPI = 32, L = 4; __VA_ARGS__; } break;                     \
+    case 192: { constexpr int TPI = 32, L = 6; __VA_ARGS__; } break;                     \
+    default: return cudaErrorInvalidValue;                                               \
+  }
+
+#define HG_DISPATCH_SPL(SP, ...)                                                         \
+  switch (SP) {                                                                          \
+    case 32: { constexpr int TP = 16, LP = 2; __VA_ARGS__; } break;                      \
+    case 64: { constexpr int TP = 16, LP = 4; __VA_ARGS__; } break;                      \
+    case 96: { constexpr int TP = 16, LP = 6; __VA_ARGS__; } break;                      \
+    default: return cudaErrorInvalidValue;                                               \
+  }

@@ -74,7 +74,8 @@ struct Slot {
   size_t bytes = 0;
   uint32_t* err_host = nullptr;
   bool busy = false;
-  bool express = false;  // runs short requests on a reserved share of every SM
+  bool express = false;      // runs short requests on a reserved share of every SM
+  bool express_dec = false;  // the express slot of short decryptions
 };
 
 size_t slice_dev_bytes(const KeyRec& k, const hg_request& r, size_t n) {
@@ -117,6 +118,7 @@ struct hg_server {
   double slice_us = 50000.0;   // most GPU time one request gets per micro-batch
   int policy = 0;              // HG_POLICY_SHORTEST or HG_POLICY_FIFO
   double express_us = -1.0;    // short-request threshold of the express slot (< 0: none)
+  size_t express_len = 0;      // > 0: short = at most this many elements, run in the latency layout
   int express_grid = 0;        // batch-kernel blocks of the express slot
   int regular_grid = 0;        // batch-kernel blocks of every other slot
   size_t regular_smem = 0;     // dynamic shared memory that keeps regular batches
@@ -229,7 +231,9 @@ void run_slot(hg_server& s, Slot& sl) {
     }
   }
   if (!specs.empty()) {
-    const BatchPlan plan = plan_batch(specs, s.variant);
+    // express batches of the length rule run in the latency layout
+    const int V = (sl.express && s.express_len > 0) ? hg::kBatchLatencyVariant : s.variant;
+    const BatchPlan plan = plan_batch(specs, V);
     const size_t jb = plan.jobs.size() * sizeof(hg::BatchJob), tb = plan.tiles.size() * sizeof(hg::BatchTile);
     auto* hj = sl.pin.take<uint8_t>(jb);
     auto* ht = sl.pin.take<uint8_t>(tb);
@@ -240,13 +244,17 @@ void run_slot(hg_server& s, Slot& sl) {
     cuda_check(cudaMemcpyAsync(dj, hj, jb, cudaMemcpyHostToDevice, st), "H2D jobs");
     cuda_check(cudaMemcpyAsync(dt, ht, tb, cudaMemcpyHostToDevice, st), "H2D tiles");
     cuda_check(cudaMemsetAsync(sl.counter.p, 0, 4, st), "memset counter");
-    const int grid = sl.express ? s.express_grid : s.regular_grid;
+    // the express slots split the reserved blocks, so neither waits for the
+    // other's blocks to retire
+    int n_express = 0;
+    for (auto& o : s.slots) n_express += o->express ? 1 : 0;
+    const int grid = sl.express ? std::max(1, s.express_grid / std::max(1, n_express)) : s.regular_grid;
     if ((size_t)grid * hg::batch_warps_per_block() * plan.warp_words * 4 > sl.scratch.n)
       fail(HG_ERR_NOMEM, "server scratch too small for this batch");
     // regular batches carry shared-memory padding that caps them below the
     // per-SM block limit, so however many overlap, every SM keeps room for
     // the express slot's blocks
-    cuda_check(hg::launch_batch(s.variant, dj, dt, (uint32_t)plan.tiles.size(), sl.counter.as<uint32_t>(),
+    cuda_check(hg::launch_batch(V, dj, dt, (uint32_t)plan.tiles.size(), sl.counter.as<uint32_t>(),
                                 sl.scratch.as<uint32_t>(), plan.warp_words, err, grid, st,
                                 sl.express ? 0 : s.regular_smem),
                "batch launch");
@@ -332,27 +340,46 @@ void scheduler(hg_server* sp) {
         return ra < rb;
       });
     bool launched = false;
-    // short requests (estimated remaining work <= express_us) belong to the
-    // express slot unless their backlog exceeds what it takes per batch
+    // class of a pending request: 0 regular, 1 express, 2 express decrypt.
+    // With express_len, short = at most express_len elements (short
+    // decryptions get their own express slot when there is one); otherwise
+    // short = estimated remaining work <= express_us.
+    bool dec_slot = false;
+    for (auto& slp : s.slots) dec_slot |= slp->express_dec;
+    auto klass = [&](const Req* q) -> int {
+      if (s.express_len > 0) {
+        if (q->r.count > s.express_len) return 0;
+        return (dec_slot && q->r.op == hg::kBatchDecrypt) ? 2 : 1;
+      }
+      if (s.express_us < 0.0) return 0;
+      const double rem = elem_cost_us(*q->k, q->r.op) * (double)(q->r.count - q->next);
+      return rem <= s.express_us ? 1 : 0;
+    };
+    // short requests belong to the express slots unless their backlog
+    // exceeds what those take per batch
     double short_backlog = 0.0;
     if (s.express_us >= 0.0)
-      for (const Req* q : s.pending) {
-        const double rem = elem_cost_us(*q->k, q->r.op) * (double)(q->r.count - q->next);
-        if (rem <= s.express_us) short_backlog += rem;
-      }
-    const double express_batch_us = 4.0 * std::max(s.express_us, 1.0);
+      for (const Req* q : s.pending)
+        if (klass(q) != 0) short_backlog += elem_cost_us(*q->k, q->r.op) * (double)(q->r.count - q->next);
+    // an express batch of the length rule holds up to 4 short requests'
+    // worth of elements; of the cost rule, 4 x express_us of work
+    const double express_batch_us =
+        s.express_len > 0 ? 1e300 : 4.0 * std::max(s.express_us, 1.0);
+    const size_t express_batch_elems = s.express_len > 0 ? 4 * s.express_len : s.cfg.max_batch_elems;
     for (auto& slp : s.slots) {
       Slot& sl = *slp;
       if (sl.busy || s.pending.empty()) continue;
       size_t elems = 0, bytes = 0;
       double cost = 0.0;
       const double batch_cap = sl.express ? express_batch_us : s.batch_us;
+      const size_t elem_cap = sl.express ? express_batch_elems : s.cfg.max_batch_elems;
+      const int slot_class = sl.express_dec ? 2 : sl.express ? 1 : 0;
       for (auto it = s.pending.begin(); it != s.pending.end();) {
         Req* q = *it;
         if (s.express_us >= 0.0) {
-          const double rem = elem_cost_us(*q->k, q->r.op) * (double)(q->r.count - q->next);
-          const bool is_short = rem <= s.express_us;
-          if ((sl.express && !is_short) || (!sl.express && is_short && short_backlog <= express_batch_us)) {
+          const int kq = klass(q);
+          const bool overflow = s.express_len == 0 && short_backlog > express_batch_us;
+          if ((sl.express && kq != slot_class) || (!sl.express && kq != 0 && !overflow)) {
             ++it;
             continue;
           }
@@ -379,7 +406,7 @@ void scheduler(hg_server* sp) {
         }
         const size_t need = slice_dev_bytes(*q->k, q->r, len);
         const bool first = sl.slices.empty();
-        if (!first && (elems + len > s.cfg.max_batch_elems || bytes + need > sl.dev.cap ||
+        if (!first && (elems + len > elem_cap || bytes + need > sl.dev.cap ||
                        s.inflight + bytes + need > s.cfg.budget_bytes || cost >= batch_cap))
           break;
         if (first && s.inflight + need > s.cfg.budget_bytes && s.inflight > 0) break;  // wait for memory

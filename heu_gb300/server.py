@@ -24,11 +24,11 @@ class Server:
     SHORTEST, FIFO = 0, 1
 
     def __init__(self, ctx, budget_bytes=0, slots=0, max_batch_elems=0, variant=0, batch_us=0.0, slice_us=0.0,
-                 policy=0, express_us=0.0, express_share=0.0):
+                 policy=0, express_us=0.0, express_share=0.0, express_len=0):
         self.ctx = ctx
         self.lib = ctx.lib
         cfg = capi.ServerConfig(budget_bytes, slots, max_batch_elems, variant, batch_us, slice_us, policy,
-                                express_us, express_share)
+                                express_us, express_share, express_len)
         h = ctypes.c_void_p()
         capi.check(self.lib.hg_server_create(ctx.handle, ctypes.byref(cfg), ctypes.byref(h)))
         self.handle = h

@@ -11,6 +11,8 @@
  *   add       heu/library/algorithms/paillier_zahlen/evaluator.cc:30-36
  *   mul       heu/library/algorithms/paillier_zahlen/evaluator.cc:99-123
  *   sum       heu/library/numpy/evaluator.cc:355-373
+ *   bucket    heu/library/numpy/evaluator.cc:403-458 (FeatureWiseBucketSum)
+ *   matmul    heu/library/numpy/evaluator.cc:208-292 (Mul + ReduceSum)
  * yacl's MontgomerySpace / BaseTable (not vendored) are restated with
  * 64-bit limbs and CIOS Montgomery multiplication; R = 2^(64*s) where s is the
  * number of 64-bit limbs of n^2 (the same radix as the engine's 32-bit R).
@@ -453,6 +455,7 @@ typedef struct {
   void* out2;
   size_t beg, end;
   int err;
+  size_t d0, d1, d2; /* shape of the reductions (rows/M, F/K, B/N) */
 } job_t;
 
 static void* worker(void* arg) {
@@ -475,20 +478,55 @@ static void* worker(void* arg) {
         if (mul_one(k, (const uint64_t*)j->a + i * s, ((const int64_t*)j->b)[i], (uint64_t*)j->out + i * s))
           j->err = 1;
         break;
+      case 4: { /* bucket sums of feature i: buckets start at the identity (GetZero) */
+        const size_t rows = j->d0, F = j->d1, B = j->d2;
+        const uint64_t* x = (const uint64_t*)j->a;
+        const uint8_t* om = (const uint8_t*)j->b;
+        uint64_t* out = (uint64_t*)j->out + i * B * s;
+        for (size_t b = 0; b < B; ++b) memcpy(out + b * s, k->R1, 8 * s);
+        for (size_t r = 0; r < rows; ++r) {
+          const size_t b = om[r * F + i];
+          if (b >= B) {
+            j->err = 1;
+            continue;
+          }
+          mont_mul(out + b * s, out + b * s, x + r * s, k->N, k->np, s);
+        }
+        break;
+      }
+      case 5: { /* output element i of MatMul: prod_kk Mul(x(row, kk), y(kk, col)) */
+        const size_t K = j->d1, N = j->d2, row = i / N, col = i % N;
+        const uint64_t* x = (const uint64_t*)j->a + row * K * s;
+        const int64_t* y = (const int64_t*)j->b;
+        uint64_t acc[MAXS], t[MAXS];
+        if (mul_one(k, x, y[col], acc)) j->err = 1;
+        for (size_t kk = 1; kk < K; ++kk) {
+          if (mul_one(k, x + kk * s, y[kk * N + col], t)) j->err = 1;
+          mont_mul(acc, acc, t, k->N, k->np, s);
+        }
+        memcpy((uint64_t*)j->out + i * s, acc, 8 * s);
+        break;
+      }
+      case 6: { /* partial product of this thread's range (numpy Sum) */
+        if (i == j->beg) memcpy(j->out2, (const uint64_t*)j->a + i * s, 8 * s);
+        else mont_mul((uint64_t*)j->out2, (const uint64_t*)j->out2, (const uint64_t*)j->a + i * s, k->N, k->np, s);
+        break;
+      }
     }
   }
   return NULL;
 }
 
-static int run(const pz_key* k, int op, const void* a, const void* b, void* out, void* out2, size_t count,
-               int threads) {
+static int run_shaped(const pz_key* k, int op, const void* a, const void* b, void* out, void* out2, size_t count,
+                      int threads, size_t d0, size_t d1, size_t d2, uint64_t* partials) {
   if (threads < 1) threads = 1;
   if ((size_t)threads > count) threads = count ? (int)count : 1;
   pthread_t th[256];
   job_t jobs[256];
   if (threads > 256) threads = 256;
   for (int t = 0; t < threads; ++t) {
-    jobs[t] = (job_t){k, op, a, b, out, out2, count * t / threads, count * (t + 1) / threads, 0};
+    jobs[t] = (job_t){k, op, a, b, out, partials ? partials + (size_t)t * k->s : out2,
+                      count * t / threads, count * (t + 1) / threads, 0, d0, d1, d2};
     pthread_create(&th[t], NULL, worker, &jobs[t]);
   }
   int err = 0;
@@ -497,6 +535,11 @@ static int run(const pz_key* k, int op, const void* a, const void* b, void* out,
     err |= jobs[t].err;
   }
   return err;
+}
+
+static int run(const pz_key* k, int op, const void* a, const void* b, void* out, void* out2, size_t count,
+               int threads) {
+  return run_shaped(k, op, a, b, out, out2, count, threads, 0, 0, 0, NULL);
 }
 
 int pz_encrypt(const pz_key* k, const int64_t* m, const uint64_t* r, uint64_t* out, size_t count, int threads) {
@@ -521,4 +564,36 @@ int pz_sum(const pz_key* k, const uint64_t* a, size_t count, uint64_t* out) {
   for (size_t i = 1; i < count; ++i) mont_mul(acc, acc, a + i * s, k->N, k->np, s);
   memcpy(out, acc, 8 * s);
   return 0;
+}
+
+/* numpy Sum over a thread pool: one partial product per thread, combined in
+ * order (parallel_reduce of numpy/evaluator.cc:355-373) */
+int pz_sum_mt(const pz_key* k, const uint64_t* a, size_t count, uint64_t* out, int threads) {
+  const int s = k->s;
+  if (count == 0) return 1;
+  if (threads < 1) threads = 1;
+  if ((size_t)threads > count) threads = (int)count;
+  if (threads > 256) threads = 256;
+  uint64_t* part = (uint64_t*)malloc((size_t)threads * s * 8);
+  if (!part) return 3;
+  const int err = run_shaped(k, 6, a, NULL, NULL, NULL, count, threads, 0, 0, 0, part);
+  memcpy(out, part, 8 * s);
+  for (int t = 1; t < threads; ++t) mont_mul(out, out, part + (size_t)t * s, k->N, k->np, s);
+  free(part);
+  return err;
+}
+
+/* FeatureWiseBucketSum of one ciphertext column x (rows) with order map om
+ * (rows x F, bin ids < B): out[f * B + b] = prod of x[r] with om[r, f] == b,
+ * the identity for empty buckets; features over the thread pool */
+int pz_bucket_sum(const pz_key* k, const uint64_t* x, size_t rows, const uint8_t* om, size_t F, size_t B,
+                  uint64_t* out, int threads) {
+  return run_shaped(k, 4, x, om, out, NULL, F, threads, rows, F, B, NULL);
+}
+
+/* MatMul out(i, j) = prod_kk Mul(x(i, kk), y(kk, j)) for x M x K ciphertexts
+ * and y K x N int64 scalars; output elements over the thread pool */
+int pz_matmul(const pz_key* k, const uint64_t* x, size_t M, size_t K, const int64_t* y, size_t N, uint64_t* out,
+              int threads) {
+  return run_shaped(k, 5, x, y, out, NULL, M * N, threads, M, K, N, NULL);
 }

@@ -30,6 +30,9 @@ def load():
             ("pz_add", [P, P, P, P, ctypes.c_size_t, ctypes.c_int]),
             ("pz_mul", [P, P, P, P, ctypes.c_size_t, ctypes.c_int]),
             ("pz_sum", [P, P, ctypes.c_size_t, P]),
+            ("pz_sum_mt", [P, P, ctypes.c_size_t, P, ctypes.c_int]),
+            ("pz_bucket_sum", [P, P, ctypes.c_size_t, P, ctypes.c_size_t, ctypes.c_size_t, P, ctypes.c_int]),
+            ("pz_matmul", [P, P, ctypes.c_size_t, ctypes.c_size_t, P, ctypes.c_size_t, P, ctypes.c_int]),
         ):
             fn = getattr(lib, name)
             fn.argtypes = args
@@ -118,4 +121,27 @@ class CKey:
     def sum(self, a):
         out = np.empty((1, self.s), dtype=np.uint64)
         assert self.lib.pz_sum(self.h, _p(a), a.shape[0], _p(out)) == 0
+        return out
+
+    def sum_mt(self, a, threads=1):
+        out = np.empty((1, self.s), dtype=np.uint64)
+        assert self.lib.pz_sum_mt(self.h, _p(np.ascontiguousarray(a)), a.shape[0], _p(out), threads) == 0
+        return out
+
+    def bucket_sum(self, x, order_map, buckets, threads=1):
+        """x (rows, s) ciphertexts, order_map (rows, F) uint8 -> (F * buckets, s)."""
+        x = np.ascontiguousarray(x)
+        om = np.ascontiguousarray(order_map, dtype=np.uint8)
+        F = om.shape[1]
+        out = np.empty((F * buckets, self.s), dtype=np.uint64)
+        assert self.lib.pz_bucket_sum(self.h, _p(x), x.shape[0], _p(om), F, buckets, _p(out), threads) == 0
+        return out
+
+    def matmul(self, x, y, threads=1):
+        """x (M, K, s) ciphertexts, y (K, N) int64 -> (M, N, s)."""
+        x = np.ascontiguousarray(x)
+        y = np.ascontiguousarray(y, dtype=np.int64)
+        M, K, N = x.shape[0], x.shape[1], y.shape[1]
+        out = np.empty((M, N, self.s), dtype=np.uint64)
+        assert self.lib.pz_matmul(self.h, _p(x), M, K, _p(y), N, _p(out), threads) == 0
         return out

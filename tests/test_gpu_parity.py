@@ -225,6 +225,7 @@ def test_mul_bigint_device_form_and_limits(kk):
     dm = torch.from_numpy(mags.view(np.int32)).cuda()
     dn = torch.from_numpy(neg).cuda()
     dout = torch.zeros_like(dc)
+    torch.cuda.synchronize()  # the engine's stream does not wait for torch's
     capi.check(key.lib.hg_dev_mul_bn(key.ctx.handle, key.id, P(dc), P(dm), P(dn), width, P(dout), 5, None))
     torch.cuda.synchronize()
     capi.check(key.lib.hg_dev_check(key.ctx.handle))
@@ -262,6 +263,36 @@ def test_ciphertext_range_rejected(kk):
         assert ei.value.code == capi.HG_ERR_CT_RANGE
 
 
+def test_latency_and_throughput_layouts_agree(gpu_key):
+    """Small batches run in the latency layout (a warp per ciphertext mod n^2,
+    a half warp per CRT side) and large ones in the throughput layout; both
+    give paillier_z's bytes (C restatement) for Encrypt, Mul and Decrypt."""
+    import os
+
+    from oracle import cref
+
+    key, pk, sk = gpu_key(2048, 0)
+    n = 12288  # above one wave of the latency layout
+    rng = np.random.default_rng(41)
+    m = rng.integers(-(2 ** 40), 2 ** 40, size=n, dtype=np.int64)
+    r = rng.integers(0, 2 ** 32, size=(n, key.r_limbs), dtype=np.uint64).astype(np.uint32)
+    k = rng.integers(-(2 ** 63), 2 ** 63 - 1, size=n, dtype=np.int64)
+    ck = cref.CKey(2048, pk, sk, window=10)
+    threads = os.cpu_count() or 1
+    want = ck.encrypt(m, np.ascontiguousarray(r).view(np.uint64), threads).view(np.uint32).reshape(n, -1)
+    big = key.encrypt(m, r)
+    for small_n in (1, 3, 64, 1000):
+        small = key.encrypt(m[:small_n], r[:small_n])
+        assert np.array_equal(small, want[:small_n]), f"latency-layout encrypt differs at n={small_n}"
+    assert np.array_equal(big, want), "throughput-layout encrypt differs"
+    want_mul = ck.mul(np.ascontiguousarray(want).view(np.uint64), k, threads).view(np.uint32).reshape(n, -1)
+    assert np.array_equal(key.mul(big[:37], k[:37]), want_mul[:37])
+    assert np.array_equal(key.mul(big, k), want_mul)
+    d_small, _ = key.decrypt(big[:29])
+    d_big, ovf = key.decrypt(big)
+    assert np.array_equal(d_small, m[:29]) and np.array_equal(d_big, m) and ovf.sum() == 0
+
+
 def test_sum_checks_every_input(gpu_key):
     """A value >= n^2 anywhere in a Sum input is rejected (evaluator.cc:21-23
     VALIDATE), not only at the first element of a reduction chunk."""
@@ -281,6 +312,7 @@ def test_sum_checks_every_input(gpu_key):
     zs[63] = hg.ints_to_limbs([pk.n2], key.ct_limbs)[0]
     d = torch.from_numpy(zs.view(np.int32)).cuda()
     out = torch.zeros((1, key.ct_limbs), dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()  # the engine's stream does not wait for torch's
     capi.check(key.lib.hg_dev_sum(key.ctx.handle, key.id, ctypes.c_void_p(d.data_ptr()), 64,
                                   ctypes.c_void_p(out.data_ptr()), None))
     torch.cuda.synchronize()

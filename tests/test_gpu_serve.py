@@ -27,11 +27,16 @@ def _alone(key, op, x0, x1):
     return key.sum(x0)
 
 
-@pytest.mark.parametrize("policy", [hg.Server.SHORTEST, hg.Server.FIFO])
-def test_served_results_equal_alone(gpu_ctx, gpu_key, policy):
+@pytest.mark.parametrize("policy,express_len", [(hg.Server.SHORTEST, 0), (hg.Server.FIFO, 0),
+                                                 (hg.Server.SHORTEST, 512)],
+                         ids=["shortest", "fifo", "latency-class"])
+def test_served_results_equal_alone(gpu_ctx, gpu_key, policy, express_len):
+    """With express_len the requests of at most 512 elements run in the two
+    express slots in the latency layout; results stay identical."""
     keys = [gpu_key(2048, 0)[0], gpu_key(3072, 2)[0], gpu_key(1024, 1)[0]]
     rng = np.random.default_rng(17)
-    server = hg.Server(gpu_ctx, budget_bytes=2 << 30, slots=3, max_batch_elems=1 << 14, policy=policy)
+    server = hg.Server(gpu_ctx, budget_bytes=2 << 30, slots=4 if express_len else 3, max_batch_elems=1 << 14,
+                       policy=policy, express_len=express_len)
     # one resident vector per key
     vec_len = 3000
     residents, res_host = [], []

@@ -252,3 +252,26 @@ def test_c_restatement_matches_python_oracle(bits, seed):
     mm = ck.mul(ct, np.array(ks), threads=2)
     assert ck.ints(mm) == [pz.to_mont(pk, pz.mul(pk, z, k)) for z, k in zip(zs, ks)]
     assert ck.ints(ck.sum(ct))[0] == pz.to_mont(pk, pz.sum_(pk, zs))
+
+
+def test_c_restatement_reductions_match_python_oracle():
+    """The C restatement's threaded Sum, FeatureWiseBucketSum and MatMul (the
+    timed CPU baseline of the reductions) equal the Python oracle."""
+    from oracle import cref
+
+    pk, sk = oracle_key(1024, 1)
+    ck = cref.CKey(1024, pk, sk)
+    rng = np.random.default_rng(21)
+    ms = rng.integers(-1000, 1000, size=48)
+    zs = [pz.encrypt(pk, int(m), r) for m, r in zip(ms, pz.r_stream(22, 48, pk.key_size // 2))]
+    x = ck.cts([pz.to_mont(pk, z) for z in zs])
+    assert ck.ints(ck.sum_mt(x, threads=5))[0] == pz.to_mont(pk, pz.sum_(pk, zs))
+    om = rng.integers(0, 6, size=(48, 3)).astype(np.uint8)
+    got = [pz.from_mont(pk, v) for v in ck.ints(ck.bucket_sum(x, om, 6, threads=2))]
+    assert got == [row[0] for row in pz.bucket_sum(pk, [[z] for z in zs], om.tolist(), 6)]
+    y = rng.integers(-50, 50, size=(8, 3))
+    y[0, 0], y[1, 1] = 0, -1
+    out = ck.matmul(x.reshape(6, 8, -1), y, threads=3)
+    cx = [[zs[i * 8 + j] for j in range(8)] for i in range(6)]
+    assert [pz.from_mont(pk, v) for v in ck.ints(out.reshape(-1, ck.s))] == \
+        [v for row in pz.matmul(pk, cx, y.tolist()) for v in row]

@@ -76,6 +76,7 @@ def test_noalloc_sum_checks_every_input(gpu_key):
     for n, bad_at in ((2, 1), (64, 63), (300_000, 1), (300_000, 12_345)):
         x = ct[:n].clone()
         x[bad_at] = n2[0]
+        torch.cuda.synchronize()  # the engine's stream does not wait for torch's
         rc = lib.hg_dev_sum_noalloc(h, key.id, _ptr(x), n, _ptr(out), None)
         assert rc == capi.HG_ERR_CT_RANGE, (n, bad_at)
     want = torch.zeros_like(out)
