@@ -61,6 +61,10 @@ SIGNATURES = {
     "hg_plain_sub": [_P, _I, _P, _P, _P, _SZ],
     "hg_mul": [_P, _I, _P, _P, _P, _SZ],
     "hg_mul_bn": [_P, _I, _P, _P, _P, _SZ, _P, _SZ],
+    "hg_encrypt_encoded": [_P, _I, _I, ctypes.c_int64, _I, _P, _P, _P, _P, _SZ],
+    "hg_decrypt_decoded": [_P, _I, _I, ctypes.c_int64, _I, _P, _P, _P, _P, _SZ],
+    "hg_dev_encrypt_encoded": [_P, _I, _I, ctypes.c_int64, _I, _P, _P, _P, _P, _SZ, _P],
+    "hg_dev_decrypt_decoded": [_P, _I, _I, ctypes.c_int64, _I, _P, _P, _P, _P, _SZ, _P],
     "hg_negate": [_P, _I, _P, _P, _SZ],
     "hg_sum": [_P, _I, _P, _SZ, _P],
     "hg_to_mont": [_P, _I, _P, _P, _SZ],
@@ -119,6 +123,7 @@ SIGNATURES = {
 _lib = None
 
 HG_OP_ENCRYPT, HG_OP_DECRYPT, HG_OP_ADD, HG_OP_MUL, HG_OP_SUM = 0, 1, 2, 3, 4
+HG_CODEC_PLAIN_I64, HG_CODEC_PLAIN_F64, HG_CODEC_BATCH_I64, HG_CODEC_BATCH_F64 = 1, 2, 3, 4
 HG_JOB_NONNEG = 1
 
 

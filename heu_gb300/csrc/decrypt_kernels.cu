@@ -19,7 +19,7 @@ __global__ void __launch_bounds__(kBlock) k_decrypt(KeyConst kc, SecConst sc, co
                                                     size_t count, int64_t* __restrict__ out_i64,
                                                     uint8_t* __restrict__ out_ovf, uint32_t* __restrict__ out_mag,
                                                     uint8_t* __restrict__ out_neg, uint32_t* __restrict__ scratch,
-                                                    uint32_t* err, unsigned long long* ctr) {
+                                                    uint32_t* err, unsigned long long* ctr, Codec cd) {
   constexpr int SP = TP * LP;
   constexpr int UPW = 32 / (2 * TP);  // ciphertexts per warp
   constexpr int UPB = kBlock / (2 * TP);
@@ -35,7 +35,7 @@ __global__ void __launch_bounds__(kBlock) k_decrypt(KeyConst kc, SecConst sc, co
     const size_t inst = wbase + unit_w;
     const bool active = inst < count;
     decrypt_one<TP, LP>(kc, sc, ct, active ? inst : count - 1, active, side, tb, ysm[unit_b], out_i64, out_ovf,
-                        out_mag, out_neg, g, err);
+                        out_mag, out_neg, g, err, cd);
   }
 }
 
@@ -80,7 +80,8 @@ static size_t latency_wave_decrypt(int Sp) {
 
 cudaError_t launch_decrypt(int Sp, const KeyConst& kc, const SecConst& sc, const uint32_t* ct, size_t count,
                            int64_t* out_i64, uint8_t* out_ovf, uint32_t* out_mag, uint8_t* out_neg,
-                           uint32_t* scratch, uint32_t* err, int grid, unsigned long long* ctr, cudaStream_t st) {
+                           uint32_t* scratch, uint32_t* err, int grid, unsigned long long* ctr, cudaStream_t st,
+                           const Codec& cd) {
   if (count == 0) return cudaSuccess;
   const cudaError_t e = cudaMemsetAsync(ctr, 0, sizeof(*ctr), st);
   if (e != cudaSuccess) return e;
@@ -90,7 +91,7 @@ cudaError_t launch_decrypt(int Sp, const KeyConst& kc, const SecConst& sc, const
   if (count <= latency_wave_decrypt(Sp) &&
       lat_blocks * (kBlock / 32) <= (size_t)grid * units_per_block_decrypt(Sp, sc.variant)) {
     HG_DISPATCH_SPL(Sp, k_decrypt<TP, LP><<<(unsigned)lat_blocks, kBlock, 0, st>>>(
-                            kc, sc, ct, count, out_i64, out_ovf, out_mag, out_neg, scratch, err, ctr));
+                            kc, sc, ct, count, out_i64, out_ovf, out_mag, out_neg, scratch, err, ctr, cd));
     count_launches(1);
     return cudaGetLastError();
   }
@@ -99,7 +100,7 @@ cudaError_t launch_decrypt(int Sp, const KeyConst& kc, const SecConst& sc, const
     const unsigned need = (unsigned)((count + upb - 1) / upb);
     const unsigned gb = (unsigned)std::min((size_t)need, (size_t)grid);
     k_decrypt<TP, LP><<<gb, kBlock, 0, st>>>(kc, sc, ct, count, out_i64, out_ovf, out_mag, out_neg, scratch, err,
-                                             ctr);
+                                             ctr, cd);
   });
   count_launches(1);
   return cudaGetLastError();

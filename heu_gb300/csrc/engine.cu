@@ -458,6 +458,41 @@ void core_encrypt(KeyRec& k, Work& w, hg::EncMode mode, const int64_t* m, const 
              "encrypt launch");
 }
 
+// Device encodings (PlainEncoder / BatchEncoder) of the C-ABI's HG_CODEC_*.
+hg::Codec make_codec(const KeyRec& k, int codec, int64_t scale, int padding, const void* in1, void* out1) {
+  if (k.scheme != 0) fail(HG_ERR_UNSUPPORTED, "device encodings serve ZPaillier keys");
+  if (codec < HG_CODEC_PLAIN_I64 || codec > HG_CODEC_BATCH_F64) fail(HG_ERR_INVALID, "unknown codec");
+  if (scale <= 0) fail(HG_ERR_INVALID, "scale must be positive");
+  const bool batch = codec == HG_CODEC_BATCH_I64 || codec == HG_CODEC_BATCH_F64;
+  if (batch && (padding < 0 || 128 + padding > 16 * k.S))
+    fail(HG_ERR_INVALID, "padding_bits must be >= 0 and leave both slots below the plaintext bound");
+  hg::Codec cd{};
+  cd.kind = codec;
+  cd.padding = batch ? padding : 0;
+  cd.scale = scale;
+  cd.in1 = in1;
+  cd.out1 = out1;
+  return cd;
+}
+
+void core_encrypt_encoded(KeyRec& k, Work& w, const void* values, const uint32_t* r, uint32_t* out, size_t count,
+                          const hg::Codec& cd) {
+  cuda_check(hg::launch_encrypt(k.S, k.kc, hg::EncMode::kEncrypt, static_cast<const int64_t*>(values), nullptr,
+                                nullptr, r, nullptr, out, count, w.errp(), 0, w.stream, cd),
+             "encrypt launch");
+}
+
+void core_decrypt_decoded(KeyRec& k, Work& w, const uint32_t* ct, void* out, uint8_t* ovf, size_t count,
+                          const hg::Codec& cd) {
+  if (!k.secret) fail(HG_ERR_NO_SECRET, "key has no secret part");
+  const size_t ntab = (size_t)1 << (k.sc.wd - 1);
+  const size_t units = (size_t)k.grid_dec * hg::units_per_block_decrypt(k.Sp, k.sc.variant);
+  uint32_t* scratch = w.scratch.ensure<uint32_t>(units * 2 * ntab * k.Sp * 4);
+  cuda_check(hg::launch_decrypt(k.Sp, k.kc, k.sc, ct, count, static_cast<int64_t*>(out), ovf, nullptr, nullptr,
+                                scratch, w.errp(), k.grid_dec, w.ctrp(), w.stream, cd),
+             "decrypt launch");
+}
+
 // Add(ct, pt) / Sub(ct, pt) with int64 plaintexts, per scheme.
 void core_add_plain(KeyRec& k, Work& w, const uint32_t* a, const int64_t* p, int neg, uint32_t* out, size_t count) {
   if (k.scheme == 1) {
@@ -1351,6 +1386,56 @@ int hg_encrypt(hg_ctx* ctx, int key_id, const int64_t* m, const uint32_t* r, uin
   });
 }
 
+int hg_encrypt_encoded(hg_ctx* ctx, int key_id, int codec, int64_t scale, int padding_bits, const void* values,
+                       const void* values2, const uint32_t* r, uint32_t* ct_out, size_t count) {
+  return guarded(__func__, [&] {
+    if (!values || !r || !ct_out) fail(HG_ERR_INVALID, "null argument");
+    if ((codec == HG_CODEC_BATCH_I64 || codec == HG_CODEC_BATCH_F64) && !values2)
+      fail(HG_ERR_INVALID, "batch encodings take two value arrays");
+    HG_HOST_PROLOGUE
+    make_codec(*k, codec, scale, padding_bits, nullptr, nullptr);  // validates before any work
+    const size_t rb = (size_t)k->kc.rlimbs * 4;
+    run_chunked(ctx, w, count, [&](Work& v, size_t off, size_t cnt) {
+      auto* dm = v.io[0].ensure<int64_t>(cnt * 8);
+      auto* dr = v.io[1].ensure<uint32_t>(cnt * rb);
+      auto* dout = v.io[2].ensure<uint32_t>(cnt * cb);
+      int64_t* dm2 = nullptr;
+      h2d(dm, static_cast<const uint8_t*>(values) + off * 8, cnt * 8, v);
+      if (values2) {
+        dm2 = v.io[3].ensure<int64_t>(cnt * 8);
+        h2d(dm2, static_cast<const uint8_t*>(values2) + off * 8, cnt * 8, v);
+      }
+      h2d(dr, (const uint8_t*)r + off * rb, cnt * rb, v);
+      core_encrypt_encoded(*k, v, dm, dr, dout, cnt, make_codec(*k, codec, scale, padding_bits, dm2, nullptr));
+      d2h((uint8_t*)ct_out + off * cb, dout, cnt * cb, v);
+    });
+    return HG_OK;
+  });
+}
+
+int hg_decrypt_decoded(hg_ctx* ctx, int key_id, int codec, int64_t scale, int padding_bits, const uint32_t* ct,
+                       void* out, void* out2, uint8_t* overflow, size_t count) {
+  return guarded(__func__, [&] {
+    if (!ct || !out) fail(HG_ERR_INVALID, "null argument");
+    const bool batch = codec == HG_CODEC_BATCH_I64 || codec == HG_CODEC_BATCH_F64;
+    if (batch && !out2) fail(HG_ERR_INVALID, "batch decodings fill two output arrays");
+    HG_HOST_PROLOGUE
+    make_codec(*k, codec, scale, padding_bits, nullptr, nullptr);
+    run_chunked(ctx, w, count, [&](Work& v, size_t off, size_t cnt) {
+      auto* dc = v.io[0].ensure<uint32_t>(cnt * cb);
+      auto* dm = v.io[1].ensure<int64_t>(cnt * 8);
+      auto* dov = v.io[2].ensure<uint8_t>(cnt);
+      int64_t* dm2 = batch ? v.io[3].ensure<int64_t>(cnt * 8) : nullptr;
+      h2d(dc, (const uint8_t*)ct + off * cb, cnt * cb, v);
+      core_decrypt_decoded(*k, v, dc, dm, dov, cnt, make_codec(*k, codec, scale, padding_bits, nullptr, dm2));
+      d2h(static_cast<uint8_t*>(out) + off * 8, dm, cnt * 8, v);
+      if (batch) d2h(static_cast<uint8_t*>(out2) + off * 8, dm2, cnt * 8, v);
+      if (overflow) d2h(overflow + off, dov, cnt, v);
+    });
+    return HG_OK;
+  });
+}
+
 int hg_encrypt_bn(hg_ctx* ctx, int key_id, const uint32_t* m_mag, const uint8_t* m_neg, const uint32_t* r,
                   uint32_t* ct_out, size_t count) {
   return guarded(__func__, [&] {
@@ -1836,6 +1921,28 @@ int hg_dev_decrypt(hg_ctx* ctx, int key_id, const uint32_t* ct, int64_t* m_out, 
   return guarded(__func__, [&] {
     HG_DEV_PROLOGUE
     core_decrypt(*k, w, ct, m_out, overflow, nullptr, nullptr, count);
+    return HG_OK;
+  });
+}
+
+int hg_dev_encrypt_encoded(hg_ctx* ctx, int key_id, int codec, int64_t scale, int padding_bits, const void* values,
+                           const void* values2, const uint32_t* r, uint32_t* ct_out, size_t count, void* stream) {
+  return guarded(__func__, [&] {
+    if ((codec == HG_CODEC_BATCH_I64 || codec == HG_CODEC_BATCH_F64) && !values2)
+      fail(HG_ERR_INVALID, "batch encodings take two value arrays");
+    HG_DEV_PROLOGUE
+    core_encrypt_encoded(*k, w, values, r, ct_out, count, make_codec(*k, codec, scale, padding_bits, values2, nullptr));
+    return HG_OK;
+  });
+}
+
+int hg_dev_decrypt_decoded(hg_ctx* ctx, int key_id, int codec, int64_t scale, int padding_bits, const uint32_t* ct,
+                           void* out, void* out2, uint8_t* overflow, size_t count, void* stream) {
+  return guarded(__func__, [&] {
+    if ((codec == HG_CODEC_BATCH_I64 || codec == HG_CODEC_BATCH_F64) && !out2)
+      fail(HG_ERR_INVALID, "batch decodings fill two output arrays");
+    HG_DEV_PROLOGUE
+    core_decrypt_decoded(*k, w, ct, out, overflow, count, make_codec(*k, codec, scale, padding_bits, nullptr, out2));
     return HG_OK;
   });
 }

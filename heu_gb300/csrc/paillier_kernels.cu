@@ -29,11 +29,11 @@ __global__ void __launch_bounds__(kBlock) k_encrypt(KeyConst kc, EncMode mode, c
                                                     const uint8_t* __restrict__ m_neg,
                                                     const uint32_t* __restrict__ r,
                                                     const uint32_t* __restrict__ ct_in, uint32_t* __restrict__ out,
-                                                    size_t count, uint32_t* err) {
+                                                    size_t count, uint32_t* err, Codec cd) {
   HG_INSTANCE_PROLOGUE(count)
   uint32_t N[L];
   load_slice<L>(N, kc.N + g.t * L);
-  encrypt_one<TPI, L>(kc, mode, m, m_mag, m_neg, r, ct_in, out, i, active, N, g, err);
+  encrypt_one<TPI, L>(kc, mode, m, m_mag, m_neg, r, ct_in, out, i, active, N, g, err, cd);
 }
 
 template <int TPI, int L>
@@ -344,17 +344,17 @@ int resident_blocks_mul(int S, int variant) {
 
 cudaError_t launch_encrypt(int S, const KeyConst& kc, EncMode mode, const int64_t* m, const uint32_t* m_mag,
                            const uint8_t* m_neg, const uint32_t* r, const uint32_t* ct_in, uint32_t* out,
-                           size_t count, uint32_t* err, int grid, cudaStream_t st) {
+                           size_t count, uint32_t* err, int grid, cudaStream_t st, const Codec& cd) {
   (void)grid;
   if (count == 0) return cudaSuccess;
   if (count <= latency_wave_encrypt(S)) {
     HG_DISPATCH_SL(S, k_encrypt<TPI, L><<<blocks_for(count, TPI), kBlock, 0, st>>>(kc, mode, m, m_mag, m_neg, r,
-                                                                                  ct_in, out, count, err));
+                                                                                  ct_in, out, count, err, cd));
     return counted();
   }
   HG_DISPATCH_SV(S, kc.variant,
                  k_encrypt<TPI, L><<<blocks_for(count, TPI), kBlock, 0, st>>>(kc, mode, m, m_mag, m_neg, r, ct_in,
-                                                                             out, count, err));
+                                                                             out, count, err, cd));
   return counted();
 }
 

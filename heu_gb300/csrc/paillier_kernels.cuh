@@ -75,11 +75,26 @@ constexpr uint16_t kOpNop = 0xFFFEu;
 
 enum class EncMode : int { kEncrypt = 0, kZero = 1, kRandomize = 2 };
 
+// Plaintext encodings applied inside the encryption and decryption kernels
+// (HEU's PlainEncoder, phe/encoding/plain_encoder.h:46-74, and BatchEncoder,
+// phe/encoding/batch_encoder.h:27-140).  Values match include/heu_gb300.h's
+// HG_CODEC_*.
+enum : int { kCodecNone = 0, kCodecPlainI64 = 1, kCodecPlainF64 = 2, kCodecBatchI64 = 3, kCodecBatchF64 = 4 };
+struct Codec {
+  int kind;         // kCodec*
+  int padding;      // BatchEncoder padding bits between the two slots
+  int64_t scale;    // > 0
+  const void* in1;  // encryption: the second slot's values (batch kinds)
+  void* out1;       // decryption: the second slot's values (batch kinds)
+};
+
 // Launchers.  All are asynchronous on `stream` and return cudaError_t of the
 // launch.  `cfg` selects the (threads per instance, limbs per thread) variant.
+// With cd.kind != kCodecNone (mode kEncrypt) `m` holds the values to encode
+// (int64 or double, per cd.kind) and m_mag / m_neg are unused.
 cudaError_t launch_encrypt(int S, const KeyConst& kc, EncMode mode, const int64_t* m, const uint32_t* m_mag,
                            const uint8_t* m_neg, const uint32_t* r, const uint32_t* ct_in, uint32_t* out,
-                           size_t count, uint32_t* err, int grid, cudaStream_t st);
+                           size_t count, uint32_t* err, int grid, cudaStream_t st, const Codec& cd = Codec{});
 cudaError_t launch_add(int S, const KeyConst& kc, const uint32_t* a, const uint32_t* b, uint32_t* out,
                        size_t count, uint32_t* err, cudaStream_t st);
 cudaError_t launch_add_plain(int S, const KeyConst& kc, const uint32_t* a, const int64_t* p, int neg_p,
@@ -98,9 +113,12 @@ cudaError_t launch_mul_bn(int S, const KeyConst& kc, const uint32_t* a, const ui
 int resident_blocks_mul_bn(int S);
 // sel[i] = neg[i] ? -1 : 1 (selector of the batch inverse)
 cudaError_t launch_sel_from_neg(const uint8_t* neg, int64_t* sel, size_t count, cudaStream_t st);
+// With cd.kind != kCodecNone out_i64 receives the decoded values (int64 or
+// double, per cd.kind) and cd.out1 the second slot of batch kinds.
 cudaError_t launch_decrypt(int Sp, const KeyConst& kc, const SecConst& sc, const uint32_t* ct, size_t count,
                            int64_t* out_i64, uint8_t* out_ovf, uint32_t* out_mag, uint8_t* out_neg,
-                           uint32_t* scratch, uint32_t* err, int grid, unsigned long long* ctr, cudaStream_t st);
+                           uint32_t* scratch, uint32_t* err, int grid, unsigned long long* ctr, cudaStream_t st,
+                           const Codec& cd = Codec{});
 // OU decryption over S-limb ciphertexts with Sp-limb p^2 arithmetic
 // (S, Sp) in {(64, 32), (128, 64), (128, 96)}.
 cudaError_t launch_ou_decrypt(int S, const KeyConst& kc, const OuConst& oc, const uint32_t* ct, size_t count,

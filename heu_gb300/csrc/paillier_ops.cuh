@@ -24,6 +24,92 @@ __device__ __forceinline__ uint32_t get_bits(const uint32_t* __restrict__ x, int
   return (uint32_t)(v >> sh) & ((w >= 32) ? 0xffffffffu : ((1u << w) - 1u));
 }
 
+// 32 bits at bit offset 32*gi of (u << sh), for any sh >= 0.
+__device__ __forceinline__ uint32_t limb_of_shifted(uint64_t u, int sh, int gi) {
+  const int off = 32 * gi - sh;
+  if (off >= 64 || off <= -32) return 0u;
+  return off >= 0 ? (uint32_t)(u >> off) : (uint32_t)(u << (-off));
+}
+
+// The plaintext of element i under a device encoding, as the pieces from
+// which its magnitude's limbs are cut: magnitude = lo + (hi << hsh) (hi may
+// be 0), sign `neg`; `bad` when the value cannot be encoded (non-finite or
+// out-of-range doubles).
+//   PlainEncoder (plain_encoder.h:58-61): int64 x -> int128(x) * scale;
+//     double x -> trunc(x * scale) as an integer of any size.
+//   BatchEncoder (batch_encoder.h:53-80, 119-126): the 64-bit two's
+//     complement patterns of a * scale and b * scale (doubles: int64(trunc(
+//     x * scale))), b's shifted up by 64 + padding bits.
+struct EncodedPlain {
+  uint64_t lo = 0, hi = 0;
+  int hsh = 64;
+  bool neg = false, bad = false;
+};
+
+__device__ __forceinline__ EncodedPlain encode_plain(const Codec& cd, const int64_t* __restrict__ m, size_t i) {
+  EncodedPlain e;
+  const double sc = (double)cd.scale;
+  switch (cd.kind) {
+    case kCodecPlainI64: {
+      const int64_t x = m[i];
+      const uint64_t a = x < 0 ? (uint64_t)0 - (uint64_t)x : (uint64_t)x;
+      const uint64_t s = (uint64_t)cd.scale;
+      e.lo = a * s;
+      e.hi = __umul64hi(a, s);
+      e.neg = x < 0 && a != 0;
+      break;
+    }
+    case kCodecPlainF64: {
+      const double d = trunc(reinterpret_cast<const double*>(m)[i] * sc);
+      if (!isfinite(d)) {
+        e.bad = true;
+        break;
+      }
+      e.neg = d < 0.0;
+      const double a = fabs(d);
+      if (a < 18446744073709551616.0) {
+        e.lo = (uint64_t)a;
+      } else {  // a = mantissa * 2^ex exactly (integer-valued, ex >= 12)
+        const uint64_t bits = (uint64_t)__double_as_longlong(a);
+        const int ex = (int)((bits >> 52) & 0x7ff) - 1075;
+        e.hi = (bits & ((1ull << 52) - 1)) | (1ull << 52);
+        e.hsh = ex;
+      }
+      break;
+    }
+    case kCodecBatchI64:
+    case kCodecBatchF64: {
+      int64_t a, b;
+      if (cd.kind == kCodecBatchI64) {
+        a = (int64_t)((uint64_t)m[i] * (uint64_t)cd.scale);
+        b = (int64_t)((uint64_t)reinterpret_cast<const int64_t*>(cd.in1)[i] * (uint64_t)cd.scale);
+      } else {
+        const double da = trunc(reinterpret_cast<const double*>(m)[i] * sc);
+        const double db = trunc(reinterpret_cast<const double*>(cd.in1)[i] * sc);
+        // static_cast<int64_t>(double) needs the value in int64's range
+        const double lim = 9223372036854775808.0;
+        if (!(da >= -lim && da < lim && db >= -lim && db < lim)) {
+          e.bad = true;
+          break;
+        }
+        a = (int64_t)da;
+        b = (int64_t)db;
+      }
+      e.lo = (uint64_t)a;
+      e.hi = (uint64_t)b;
+      e.hsh = 64 + cd.padding;
+      break;
+    }
+    default:
+      break;
+  }
+  return e;
+}
+
+__device__ __forceinline__ uint32_t encoded_limb(const EncodedPlain& e, int gi) {
+  return limb_of_shifted(e.lo, 0, gi) | limb_of_shifted(e.hi, e.hsh, gi);
+}
+
 // gm = Montgomery form of (1 + m*n) mod N for m = (neg ? -A : A), A < n:
 //   X = MM(A, n*R^2) = A*n*R;  gm = R + X (m >= 0) or R + (N - X) (m < 0).
 template <int TPI, int L>
@@ -55,13 +141,32 @@ __device__ __forceinline__ void encrypt_one(const KeyConst& kc, EncMode mode, co
                                             const uint32_t* __restrict__ m_mag, const uint8_t* __restrict__ m_neg,
                                             const uint32_t* __restrict__ r, const uint32_t* __restrict__ ct_in,
                                             uint32_t* __restrict__ out, size_t i, bool active,
-                                            const uint32_t (&N)[L], const Group<TPI>& g, uint32_t* err) {
+                                            const uint32_t (&N)[L], const Group<TPI>& g, uint32_t* err,
+                                            const Codec& cd = Codec{}) {
   constexpr int S = TPI * L;
   uint32_t acc[L];
   if (mode == EncMode::kEncrypt) {
     uint32_t A[L];
     bool neg;
-    if (m_mag != nullptr) {
+    if (cd.kind != kCodecNone) {
+      // encoded on the device; |m| <= n/2 as for any plaintext (encryptor.cc:38-40)
+      const EncodedPlain e = encode_plain(cd, m, i);
+      uint32_t NH[L], d[L];
+#pragma unroll
+      for (int j = 0; j < L; ++j) {
+        const int gi = (int)g.t * L + j;
+        A[j] = gi < S / 2 ? encoded_limb(e, gi) : 0u;
+        NH[j] = gi < S / 2 ? kc.nhalf[gi] : 0u;
+      }
+      neg = e.neg;
+      const bool too_big = sub_full<TPI, L>(d, NH, A, g) != 0u;
+      if (active && (too_big || e.bad) && g.t == 0) atomicOr(err, kErrPtRange);
+      // a value that does not fit is replaced by 0 (its error is reported)
+      if (too_big || e.bad) {
+#pragma unroll
+        for (int j = 0; j < L; ++j) A[j] = 0u;
+      }
+    } else if (m_mag != nullptr) {
       // |m| has S/2 limbs; lanes above them hold zeros
       uint32_t NH[L], d[L];
       if (g.t * L < S / 2) {
@@ -360,11 +465,98 @@ __device__ __forceinline__ uint32_t s_sub(uint32_t* r, const uint32_t* a, const 
 
 // Serial CRT tail for one ciphertext, run by one lane: y[0], y[1] = the
 // Z-form values c^(p-1) mod p^2 and c^(q-1) mod q^2 (SP = 2H limbs each).
+// Decoding of a decrypted plaintext (magnitude mm of W limbs, negative when
+// `neg`) under a device encoding, into out0 / cd.out1 (element i) and the
+// overflow flag:
+//   PlainEncoder::Decode (plain_encoder.h:64-69): int64 -> m / scale with
+//     C++ division (toward zero), flagged when it does not fit int64;
+//     double -> double(m) rounded to nearest-even, / scale (flagged, +-inf,
+//     beyond the double range).
+//   BatchEncoder::Decode (batch_encoder.h:85-103): slot s = the low 64 bits
+//     of m >> s * (64 + padding) as int64 (the sign of m applied as BigInt
+//     shifts and GetValue do: on the magnitude), / scale (int64 division, or
+//     double division for the double kind); flagged when m < 0.
+template <int W>
+__device__ void decode_plain(const Codec& cd, const uint32_t* mm, bool neg, size_t i, void* out0, uint8_t* ovf) {
+  if (cd.kind == kCodecPlainI64) {
+    bool wide = false;
+#pragma unroll 1
+    for (int j = 4; j < W; ++j) wide |= mm[j] != 0u;
+    const unsigned __int128 mag = (unsigned __int128)((uint64_t)mm[0] | ((uint64_t)mm[1] << 32)) |
+                                  ((unsigned __int128)((uint64_t)mm[2] | ((uint64_t)mm[3] << 32)) << 64);
+    const unsigned __int128 q = mag / (unsigned __int128)(uint64_t)cd.scale;
+    const bool fits = !wide && (q < ((unsigned __int128)1 << 63) || (neg && q == ((unsigned __int128)1 << 63)));
+    const uint64_t q64 = (uint64_t)q;
+    reinterpret_cast<int64_t*>(out0)[i] = fits ? (int64_t)(neg ? (uint64_t)0 - q64 : q64) : 0;
+    if (ovf) ovf[i] = fits ? 0 : 1;
+    return;
+  }
+  if (cd.kind == kCodecPlainF64) {
+    int top = -1;
+#pragma unroll 1
+    for (int j = W - 1; j >= 0 && top < 0; --j)
+      if (mm[j] != 0u) top = j;
+    double d = 0.0;
+    if (top >= 0) {
+      const int p = 32 * top + 31 - __clz(mm[top]);  // position of the top bit
+      if (p < 64) {
+        d = __ull2double_rn((uint64_t)mm[0] | ((uint64_t)(W > 1 ? mm[1] : 0u) << 32));
+      } else {
+        // the 64 bits below and including the top bit, the rest as a sticky bit
+        const int lo = p - 63;
+        uint64_t v = 0;
+#pragma unroll 1
+        for (int j = 0; j < W; ++j) {
+          const int off = 32 * j - lo;  // bit position of limb j inside v
+          if (off >= 64 || off <= -32) continue;
+          v |= off >= 0 ? ((uint64_t)mm[j] << off) : ((uint64_t)mm[j] >> (-off));
+        }
+        bool sticky = false;
+#pragma unroll 1
+        for (int j = 0; j < W && 32 * j < lo; ++j) {
+          const int keep = lo - 32 * j;  // bits of limb j below lo
+          const uint32_t below = keep >= 32 ? mm[j] : (mm[j] & ((1u << keep) - 1u));
+          sticky |= below != 0u;
+        }
+        d = ldexp(__ull2double_rn(v | (sticky ? 1ull : 0ull)), lo);
+      }
+    }
+    d = neg ? -d : d;
+    reinterpret_cast<double*>(out0)[i] = __ddiv_rn(d, (double)cd.scale);
+    if (ovf) ovf[i] = isinf(d) ? 1 : 0;
+    return;
+  }
+  // batch kinds: two slots
+#pragma unroll 1
+  for (int slot = 0; slot < 2; ++slot) {
+    const int sh = slot * (64 + cd.padding);
+    uint64_t v = 0;
+#pragma unroll 1
+    for (int j = 0; j < W; ++j) {
+      const int off = 32 * j - sh;
+      if (off >= 64 || off <= -32) continue;
+      v |= off >= 0 ? ((uint64_t)mm[j] << off) : ((uint64_t)mm[j] >> (-off));
+    }
+    const int64_t x = neg ? (int64_t)((uint64_t)0 - v) : (int64_t)v;
+    void* dst = slot == 0 ? out0 : cd.out1;
+    if (cd.kind == kCodecBatchI64) {
+      // C++ int64 division truncates toward zero
+      const uint64_t a = x < 0 ? (uint64_t)0 - (uint64_t)x : (uint64_t)x;
+      const uint64_t q = a / (uint64_t)cd.scale;
+      reinterpret_cast<int64_t*>(dst)[i] = x < 0 ? (int64_t)((uint64_t)0 - q) : (int64_t)q;
+    } else {
+      reinterpret_cast<double*>(dst)[i] = __ddiv_rn((double)x, (double)cd.scale);
+    }
+  }
+  // a negative packed plaintext means a slot underflowed its padding
+  if (ovf) ovf[i] = neg ? 1 : 0;
+}
+
 template <int H>
 __device__ __noinline__ void crt_tail(const KeyConst& kc, const SecConst& sc, const uint32_t* y0,
                                       const uint32_t* y1, size_t i, bool active, int64_t* __restrict__ out_i64,
                                       uint8_t* __restrict__ out_ovf, uint32_t* __restrict__ out_mag,
-                                      uint8_t* __restrict__ out_neg) {
+                                      uint8_t* __restrict__ out_neg, const Codec& cd) {
   uint32_t Lv[H], mp[H], mq[H], t1[H];
   // L_p = (y_p - 1)/p exactly = ((y_p - 1) mod 2^(32H)) * p^-1 mod 2^(32H)
 #pragma unroll 1
@@ -457,6 +649,10 @@ __device__ __noinline__ void crt_tail(const KeyConst& kc, const SecConst& sc, co
       mm[j] = (uint32_t)v;
     }
   }
+  if (active && cd.kind != kCodecNone) {
+    decode_plain<2 * H>(cd, mm, gt, i, out_i64, out_ovf);
+    return;
+  }
   if (active) {
     if (out_mag) {
 #pragma unroll 1
@@ -488,7 +684,8 @@ __device__ __forceinline__ void decrypt_one(const KeyConst& kc, const SecConst& 
                                             size_t i, bool active, int side, uint32_t* __restrict__ tb,
                                             uint32_t* ysm, int64_t* __restrict__ out_i64,
                                             uint8_t* __restrict__ out_ovf, uint32_t* __restrict__ out_mag,
-                                            uint8_t* __restrict__ out_neg, const Group<TP>& g, uint32_t* err) {
+                                            uint8_t* __restrict__ out_neg, const Group<TP>& g, uint32_t* err,
+                                            const Codec& cd = Codec{}) {
   constexpr int SP = TP * LP;
   const int ntab = 1 << (sc.wd - 1);
   uint32_t N[LP];
@@ -540,7 +737,8 @@ __device__ __forceinline__ void decrypt_one(const KeyConst& kc, const SecConst& 
 #pragma unroll
   for (int j = 0; j < LP; ++j) ysm[side * SP + g.t * LP + j] = acc[j];
   __syncwarp();
-  if (side == 0 && g.t == 0) crt_tail<SP / 2>(kc, sc, ysm, ysm + SP, i, active, out_i64, out_ovf, out_mag, out_neg);
+  if (side == 0 && g.t == 0)
+    crt_tail<SP / 2>(kc, sc, ysm, ysm + SP, i, active, out_i64, out_ovf, out_mag, out_neg, cd);
   __syncwarp();
 }
 

@@ -200,6 +200,37 @@ class Key:
                                           len(ms)))
         return out
 
+    def encrypt_encoded(self, codec, scale, values, r, values2=None, padding_bits=32):
+        """Encrypt raw int64 / double values encoded on the device (HG_CODEC_*:
+        PlainEncoder, plain_encoder.h:46-74; BatchEncoder, batch_encoder.h:
+        27-140, with values2 as the second slot)."""
+        f64 = codec in (capi.HG_CODEC_PLAIN_F64, capi.HG_CODEC_BATCH_F64)
+        dt = np.float64 if f64 else np.int64
+        v = np.ascontiguousarray(values, dtype=dt).reshape(-1)
+        v2 = None if values2 is None else np.ascontiguousarray(values2, dtype=dt).reshape(-1)
+        if v2 is not None and v2.size != v.size:
+            raise ValueError("both slots need the same number of values")
+        r = _u32(r).reshape(-1, self.r_limbs)
+        out = self._out(v.size)
+        capi.check(self.lib.hg_encrypt_encoded(self.ctx.handle, self.id, codec, int(scale), int(padding_bits), _ptr(v),
+                                               _ptr(v2), _ptr(r), _ptr(out), v.size))
+        return out
+
+    def decrypt_decoded(self, codec, scale, ct, padding_bits=32):
+        """Decrypt and decode on the device -> (values, overflow) or, for the
+        batch codecs, (slot0, slot1, overflow)."""
+        ct = self._ct(ct)
+        n = ct.shape[0]
+        f64 = codec in (capi.HG_CODEC_PLAIN_F64, capi.HG_CODEC_BATCH_F64)
+        dt = np.float64 if f64 else np.int64
+        out = np.empty(n, dtype=dt)
+        batch = codec in (capi.HG_CODEC_BATCH_I64, capi.HG_CODEC_BATCH_F64)
+        out2 = np.empty(n, dtype=dt) if batch else None
+        ovf = np.empty(n, dtype=np.uint8)
+        capi.check(self.lib.hg_decrypt_decoded(self.ctx.handle, self.id, codec, int(scale), int(padding_bits),
+                                               _ptr(ct), _ptr(out), _ptr(out2), _ptr(ovf), n))
+        return (out, out2, ovf) if batch else (out, ovf)
+
     def encrypt_zero(self, r):
         r = _u32(r).reshape(-1, self.r_limbs)
         out = self._out(r.shape[0])

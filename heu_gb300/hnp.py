@@ -85,6 +85,93 @@ class PlaintextArray:
     __repr__ = __str__
 
 
+class EncodedArray(PlaintextArray):
+    """hnp.array(values, encoder) for an IntegerEncoder / FloatEncoder: the
+    raw values and their encoder.  Encryption encodes them on the device
+    (the engine's PlainEncoder codec), so no host encode pass runs; the
+    encoded integers are computed on the host only if ``values`` is read."""
+
+    def __init__(self, raw, encoder):
+        self.raw = np.asarray(raw)
+        self.encoder = encoder
+        self._values = None
+
+    @property
+    def values(self):
+        if self._values is None:
+            self._values = _as_values(self.encoder.encode(self.raw))
+        return self._values
+
+    @property
+    def shape(self):
+        return self.raw.shape
+
+    @property
+    def ndim(self):
+        return self.raw.ndim
+
+    @property
+    def size(self):
+        return self.raw.size
+
+    def __getitem__(self, item):
+        return EncodedArray(self.raw[item], self.encoder)
+
+    def device_codec(self):
+        """(codec, raw values) when the device can encode them, else None."""
+        if type(self.encoder) not in (IntegerEncoder, FloatEncoder):
+            return None
+        if self.raw.dtype.kind == "f":
+            return engine.capi.HG_CODEC_PLAIN_F64, self.raw.astype(np.float64)
+        if self.raw.dtype.kind in "iu" and (self.raw.size == 0 or (int(self.raw.max()) < 2 ** 63 and
+                                                                    int(self.raw.min()) >= -(2 ** 63))):
+            return engine.capi.HG_CODEC_PLAIN_I64, self.raw.astype(np.int64)
+        return None
+
+
+class DecryptedArray(PlaintextArray):
+    """Decryptor.decrypt's result: the plaintexts of a ciphertext array,
+    decrypted when ``values`` is read; ``to_numpy(encoder)`` with an
+    IntegerEncoder / FloatEncoder decrypts and decodes in one device pass
+    (the engine's PlainEncoder codec)."""
+
+    def __init__(self, decryptor, ct):
+        self._dec = decryptor
+        self._ct = ct
+        self._values = None
+
+    @property
+    def values(self):
+        if self._values is None:
+            self._values = self._dec._decrypt_values(self._ct)
+        return self._values
+
+    @property
+    def shape(self):
+        return self._ct.shape
+
+    @property
+    def ndim(self):
+        return self._ct.ndim
+
+    @property
+    def size(self):
+        return self._ct.size
+
+    def __getitem__(self, item):
+        return DecryptedArray(self._dec, self._ct[item])
+
+    def to_numpy(self, encoder=None):
+        kit = self._dec.kit
+        if (encoder is not None and type(encoder) in (IntegerEncoder, FloatEncoder) and kit.schema == "zpaillier"
+                and self._values is None and self._ct.size > 0):
+            codec = engine.capi.HG_CODEC_PLAIN_F64 if type(encoder) is FloatEncoder else engine.capi.HG_CODEC_PLAIN_I64
+            out, ovf = kit.key.decrypt_decoded(codec, encoder.scale, self._ct.limbs)
+            if not ovf.any():
+                return out.reshape(self.shape)
+        return super().to_numpy(encoder)
+
+
 class CiphertextArray:
     """Ciphertext tensor: limbs (size, S) in Montgomery form plus a shape."""
 
@@ -218,16 +305,22 @@ class BatchEncoder:
     per pair of values."""
 
     def __init__(self, scale=1, padding_bits=32):
-        if padding_bits % 32:
-            raise ValueError("padding_bits must be a multiple of 32 here (limb-aligned packing)")
+        if padding_bits < 0:
+            raise ValueError("padding_bits must be >= 0")
         self.scale = int(scale)
         self.padding_bits = int(padding_bits)
 
     def _limbs_needed(self):
-        return (128 + self.padding_bits) // 32
+        return (128 + self.padding_bits + 31) // 32
+
+    def _aligned(self):
+        if self.padding_bits % 32:
+            raise ValueError("host packing needs padding_bits a multiple of 32 (the device codec takes any)")
 
     def pack(self, first, second, pt_limbs):
-        """int64 arrays -> (count, pt_limbs) uint32 magnitudes."""
+        """int64 arrays -> (count, pt_limbs) uint32 magnitudes (host form of
+        the device codec HG_CODEC_BATCH_I64)."""
+        self._aligned()
         a = (np.asarray(first, dtype=np.int64) * self.scale).astype(np.int64).view(np.uint64)
         b = (np.asarray(second, dtype=np.int64) * self.scale).astype(np.int64).view(np.uint64)
         if a.shape != b.shape:
@@ -248,6 +341,7 @@ class BatchEncoder:
         divided by the scale (Decode, batch_encoder.h:85-103)."""
         if index not in (0, 1):
             raise ValueError("You cannot get more than two elements from one plaintext")
+        self._aligned()
         off = index * ((64 + self.padding_bits) // 32)
         lo = mags[:, off].astype(np.uint64)
         hi = mags[:, off + 1].astype(np.uint64)
@@ -368,6 +462,8 @@ class HeKit:
     def array(self, values, encoder=None):
         """hnp.array(ndarray, encoder): values encoded by ``encoder`` when one
         is given (integers as they are otherwise)."""
+        if encoder is not None and type(encoder) in (IntegerEncoder, FloatEncoder):
+            return EncodedArray(values, encoder)
         return PlaintextArray(encoder.encode(values) if encoder is not None else values)
 
     def integer_encoder(self, scale=1):
@@ -419,6 +515,12 @@ class Encryptor:
     def _encrypt(self, pt):
         pt = pt if isinstance(pt, PlaintextArray) else PlaintextArray(pt)
         key = self.kit.key
+        dc = pt.device_codec() if isinstance(pt, EncodedArray) and self.kit.schema == "zpaillier" else None
+        if dc is not None:
+            codec, raw = dc
+            r = self._r(raw.size)
+            limbs = key.encrypt_encoded(codec, pt.encoder.scale, raw.reshape(-1), r)
+            return CiphertextArray(self.kit, limbs, pt.shape), pt, r
         flat = pt.values.reshape(-1)
         r = self._r(flat.size)
         if flat.dtype == object:
@@ -451,8 +553,19 @@ class Encryptor:
         return CiphertextArray(self.kit, self.kit.key.encrypt_zero(self._r(count)), shape)
 
     def encrypt_batch(self, first, second, encoder):
-        """Encrypt pairs packed by a BatchEncoder -> CiphertextArray of first's shape."""
+        """Encrypt pairs packed by a BatchEncoder -> CiphertextArray of first's
+        shape; ZPaillier keys pack on the device (HG_CODEC_BATCH_I64 / _F64)."""
         key = self.kit.key
+        a, b = np.asarray(first), np.asarray(second)
+        if a.shape != b.shape:
+            raise ValueError("first and second must have the same shape")
+        if self.kit.schema == "zpaillier":
+            f64 = a.dtype.kind == "f" or b.dtype.kind == "f"
+            codec = engine.capi.HG_CODEC_BATCH_F64 if f64 else engine.capi.HG_CODEC_BATCH_I64
+            r = self._r(a.size)
+            out = key.encrypt_encoded(codec, encoder.scale, a.reshape(-1), r, values2=b.reshape(-1),
+                                      padding_bits=encoder.padding_bits)
+            return CiphertextArray(self.kit, out, a.shape)
         mags = encoder.pack(first, second, key.pt_limbs)
         neg = np.zeros(mags.shape[0], dtype=np.uint8)
         r = self._r(mags.shape[0])
@@ -469,17 +582,30 @@ class Decryptor:
         self.kit = kit
 
     def decrypt(self, ct):
+        """Decrypt (numpy/decryptor.cc:19-66): the plaintexts, decrypted on
+        first use; to_numpy(encoder) on the result decodes on the device."""
+        return DecryptedArray(self, ct)
+
+    def _decrypt_values(self, ct):
         key = self.kit.key
         m, ovf = key.decrypt(ct.limbs)
         if ovf.any():
             vals = np.empty(ct.size, dtype=object)
             vals[:] = key.decrypt_bn(ct.limbs)
-            return PlaintextArray(vals.reshape(ct.shape))
-        return PlaintextArray(m.reshape(ct.shape))
+            return _as_values(vals.reshape(ct.shape))
+        return _as_values(m.reshape(ct.shape))
 
-    def decrypt_batch(self, ct, encoder):
-        """Decrypt packed ciphertexts -> (first, second) int64 arrays."""
+    def decrypt_batch(self, ct, encoder, as_float=False):
+        """Decrypt packed ciphertexts -> (first, second) int64 arrays (float64
+        with as_float, BatchEncoder::Decode<double>); ZPaillier keys unpack
+        on the device."""
         key = self.kit.key
+        if self.kit.schema == "zpaillier":
+            codec = engine.capi.HG_CODEC_BATCH_F64 if as_float else engine.capi.HG_CODEC_BATCH_I64
+            s0, s1, neg = key.decrypt_decoded(codec, encoder.scale, ct.limbs, padding_bits=encoder.padding_bits)
+            if neg.any():
+                raise ValueError("packed plaintext is negative: a slot underflowed its padding")
+            return s0.reshape(ct.shape), s1.reshape(ct.shape)
         mag = np.empty((ct.size, key.pt_limbs), dtype=np.uint32)
         neg = np.empty(ct.size, dtype=np.uint8)
         engine.capi.check(key.lib.hg_decrypt_bn(key.ctx.handle, key.id, engine._ptr(ct.limbs), engine._ptr(mag),

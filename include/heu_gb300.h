@@ -121,6 +121,34 @@ int hg_randomize(hg_ctx* ctx, int key_id, uint32_t* ct, const uint32_t* r, size_
 int hg_decrypt(hg_ctx* ctx, int key_id, const uint32_t* ct, int64_t* m_out, uint8_t* overflow, size_t count);
 int hg_decrypt_bn(hg_ctx* ctx, int key_id, const uint32_t* ct, uint32_t* m_mag, uint8_t* m_neg, size_t count);
 
+/* ---- plaintext encodings on the device ----------------------------------
+ * HEU's PlainEncoder (phe/encoding/plain_encoder.h:46-74, pylib's
+ * IntegerEncoder / FloatEncoder) and BatchEncoder (phe/encoding/
+ * batch_encoder.h:27-140) run inside the encryption and decryption kernels,
+ * so raw int64 / double values go in and out with no host encode pass.
+ *   HG_CODEC_PLAIN_I64: value * scale (exact 128-bit product); decode
+ *     m / scale with C++ division (toward zero), flagged in `overflow` when
+ *     it does not fit int64.
+ *   HG_CODEC_PLAIN_F64: trunc(value * scale) as an integer of any size
+ *     (non-finite values fail with HG_ERR_PT_RANGE); decode double(m)
+ *     (nearest-even) / scale, flagged when beyond the double range.
+ *   HG_CODEC_BATCH_I64 / _F64: two values per plaintext, (b * scale) <<
+ *     (64 + padding_bits) | (a * scale) on 64-bit two's complement patterns
+ *     (doubles: int64(trunc(x * scale))); decode slot s = the low 64 bits of
+ *     m >> s * (64 + padding_bits) as int64, / scale (int64 division, or
+ *     double division for _F64), slot 0 into `out`, slot 1 into `out2`.
+ * `values` / `out` hold int64 or double per the codec (8 bytes each);
+ * values2 / out2 are the second slots (batch codecs only).  Plaintexts above
+ * n/2 fail with HG_ERR_PT_RANGE as in hg_encrypt.  ZPaillier keys only. */
+#define HG_CODEC_PLAIN_I64 1
+#define HG_CODEC_PLAIN_F64 2
+#define HG_CODEC_BATCH_I64 3
+#define HG_CODEC_BATCH_F64 4
+int hg_encrypt_encoded(hg_ctx* ctx, int key_id, int codec, int64_t scale, int padding_bits, const void* values,
+                       const void* values2, const uint32_t* r, uint32_t* ct_out, size_t count);
+int hg_decrypt_decoded(hg_ctx* ctx, int key_id, int codec, int64_t scale, int padding_bits, const uint32_t* ct,
+                       void* out, void* out2, uint8_t* overflow, size_t count);
+
 /* ---- evaluator (replaces gpu_paillier_e_add / e_add_const / sub_ct /
  * sub_ctpt / sub_ptct / e_mul_const / e_inverse, gpupaillier.h:57-90) ---- */
 int hg_add(hg_ctx* ctx, int key_id, const uint32_t* a, const uint32_t* b, uint32_t* out, size_t count);
@@ -292,6 +320,10 @@ int hg_dev_add(hg_ctx* ctx, int key_id, const uint32_t* a, const uint32_t* b, ui
                void* stream);
 int hg_dev_mul(hg_ctx* ctx, int key_id, const uint32_t* a, const int64_t* k, uint32_t* out, size_t count,
                void* stream);
+int hg_dev_encrypt_encoded(hg_ctx* ctx, int key_id, int codec, int64_t scale, int padding_bits, const void* values,
+                           const void* values2, const uint32_t* r, uint32_t* ct_out, size_t count, void* stream);
+int hg_dev_decrypt_decoded(hg_ctx* ctx, int key_id, int codec, int64_t scale, int padding_bits, const uint32_t* ct,
+                           void* out, void* out2, uint8_t* overflow, size_t count, void* stream);
 int hg_dev_mul_bn(hg_ctx* ctx, int key_id, const uint32_t* a, const uint32_t* k_mag, const uint8_t* k_neg,
                   size_t k_limbs, uint32_t* out, size_t count, void* stream);
 int hg_dev_sum(hg_ctx* ctx, int key_id, const uint32_t* a, size_t count, uint32_t* out, void* stream);
