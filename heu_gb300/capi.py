@@ -61,6 +61,7 @@ SIGNATURES = {
     "hg_plain_sub": [_P, _I, _P, _P, _P, _SZ],
     "hg_mul": [_P, _I, _P, _P, _P, _SZ],
     "hg_mul_bn": [_P, _I, _P, _P, _P, _SZ, _P, _SZ],
+    "hg_convert_radix": [_P, _I, _P, _P, _SZ, ctypes.c_uint32, _I],
     "hg_encrypt_encoded": [_P, _I, _I, ctypes.c_int64, _I, _P, _P, _P, _P, _SZ],
     "hg_decrypt_decoded": [_P, _I, _I, ctypes.c_int64, _I, _P, _P, _P, _P, _SZ],
     "hg_dev_encrypt_encoded": [_P, _I, _I, ctypes.c_int64, _I, _P, _P, _P, _P, _SZ, _P],

@@ -207,6 +207,17 @@ class PublicKey {
   std::string ToString() const { return "GB300 Z-paillier PK: n=" + n_.ToHexString(); }
   size_t Limbs() const { return (key_size_ + 31) / 32 * 2; }  // 32-bit limbs of n^2
   size_t KeyBits() const { return Limbs() * 16; }
+
+  // Montgomery radix 2^bits of the yacl BigInt backend the HEU build uses
+  // for Ciphertext::c_ (0 = this engine's 2^(32 * Limbs()), which is the
+  // radix of the 64-bit-limb OpenSSL and GMP backends; libtommath's 60-bit
+  // digits give 2^(60 * ceil(bits(n^2) / 60))).  Ciphertexts cross the
+  // adapter in that radix and are converted on the GPU (hg_convert_radix).
+  void SetBackendRadixBits(size_t bits) { radix_bits_ = bits; }
+  size_t BackendRadixBits() const { return radix_bits_ ? radix_bits_ : 32 * Limbs(); }
+
+ private:
+  size_t radix_bits_ = 0;
 };
 
 class SecretKey {
@@ -260,6 +271,14 @@ inline std::vector<uint32_t> DrawR(const PublicKey& pk, size_t count) {
   return r;
 }
 
+// Ciphertext limbs between the backend's radix and the engine's.
+inline void ConvertRadix(const PublicKey& pk, std::vector<uint32_t>* v, bool to_backend) {
+  const size_t S = pk.Limbs();
+  if (pk.BackendRadixBits() == 32 * S || v->empty()) return;
+  Check(hg_convert_radix(Engine::Get().ctx, KeyId(pk, nullptr), v->data(), v->data(), v->size() / S,
+                         (uint32_t)pk.BackendRadixBits(), to_backend ? 1 : 0));
+}
+
 inline std::vector<uint32_t> CtLimbs(const PublicKey& pk, ConstSpan<Ciphertext> cts) {
   const size_t S = pk.Limbs();
   std::vector<uint32_t> v(cts.size() * S);
@@ -267,10 +286,13 @@ inline std::vector<uint32_t> CtLimbs(const PublicKey& pk, ConstSpan<Ciphertext> 
     if (cts[i]->c_.IsNegative()) throw std::invalid_argument("Evaluator: Invalid ciphertext");
     ToLimbs(cts[i]->c_.Mag(), &v[i * S], S);
   }
+  ConvertRadix(pk, &v, false);
   return v;
 }
 
-inline std::vector<Ciphertext> ToCts(const std::vector<uint32_t>& v, size_t S) {
+inline std::vector<Ciphertext> ToCts(const PublicKey& pk, std::vector<uint32_t> v) {
+  const size_t S = pk.Limbs();
+  ConvertRadix(pk, &v, true);
   std::vector<Ciphertext> out(v.size() / S);
   for (size_t i = 0; i < out.size(); ++i) out[i].c_ = BigInt::FromMag(FromLimbs(&v[i * S], S), false);
   return out;
@@ -347,24 +369,24 @@ class Encryptor {
     std::vector<uint32_t> ct((size_t)size * pk_.Limbs());
     detail::Check(hg_encrypt_zero(detail::Engine::Get().ctx, detail::KeyId(pk_, nullptr), r.data(), ct.data(),
                                   (size_t)size));
-    return detail::ToCts(ct, pk_.Limbs());
+    return detail::ToCts(pk_, ct);
   }
 
   std::vector<Ciphertext> Encrypt(ConstSpan<Plaintext> pts) const {
     detail::CheckPlaintexts(pk_, pts);
     const auto r = detail::DrawR(pk_, pts.size());
-    return detail::ToCts(detail::EncryptLimbs(pk_, pts, r.data()), pk_.Limbs());
+    return detail::ToCts(pk_, detail::EncryptLimbs(pk_, pts, r.data()));
   }
 
   // encryptor.cc:51-53 audit string: "p:{m},rn:{h_s^r},c:{c}"
   std::pair<std::vector<Ciphertext>, std::vector<std::string>> EncryptWithAudit(ConstSpan<Plaintext> pts) const {
     detail::CheckPlaintexts(pk_, pts);
     const auto r = detail::DrawR(pk_, pts.size());
-    auto cts = detail::ToCts(detail::EncryptLimbs(pk_, pts, r.data()), pk_.Limbs());
+    auto cts = detail::ToCts(pk_, detail::EncryptLimbs(pk_, pts, r.data()));
     std::vector<uint32_t> rn(pts.size() * pk_.Limbs());
     detail::Check(hg_encrypt_zero(detail::Engine::Get().ctx, detail::KeyId(pk_, nullptr), r.data(), rn.data(),
                                   pts.size()));
-    const auto rns = detail::ToCts(rn, pk_.Limbs());
+    const auto rns = detail::ToCts(pk_, rn);
     std::vector<std::string> audit;
     for (size_t i = 0; i < pts.size(); ++i)
       audit.push_back("p:" + pts[i]->ToHexString() + ",rn:" + rns[i].c_.ToHexString() + ",c:" +
@@ -416,7 +438,7 @@ class Evaluator {
     auto c = detail::CtLimbs(pk_, ConstSpan<Ciphertext>(in));
     const auto r = detail::DrawR(pk_, cts.size());
     detail::Check(hg_randomize(ctx(), id(), c.data(), r.data(), cts.size()));
-    auto out = detail::ToCts(c, pk_.Limbs());
+    auto out = detail::ToCts(pk_, c);
     for (size_t i = 0; i < cts.size(); ++i) *cts[i] = std::move(out[i]);
   }
 
@@ -425,7 +447,7 @@ class Evaluator {
     const auto x = detail::CtLimbs(pk_, a), y = detail::CtLimbs(pk_, b);
     std::vector<uint32_t> out(x.size());
     detail::Check(hg_add(ctx(), id(), x.data(), y.data(), out.data(), a.size()));
-    return detail::ToCts(out, pk_.Limbs());
+    return detail::ToCts(pk_, out);
   }
   std::vector<Ciphertext> Add(ConstSpan<Ciphertext> a, ConstSpan<Plaintext> b) const {
     SameSize(a.size(), b.size());
@@ -443,7 +465,7 @@ class Evaluator {
       const auto g = detail::EncryptLimbs(pk_, b, r0.data());
       detail::Check(hg_add(ctx(), id(), x.data(), g.data(), out.data(), a.size()));
     }
-    return detail::ToCts(out, pk_.Limbs());
+    return detail::ToCts(pk_, out);
   }
   std::vector<Ciphertext> Add(ConstSpan<Plaintext> a, ConstSpan<Ciphertext> b) const { return Add(b, a); }
   std::vector<Plaintext> Add(ConstSpan<Plaintext> a, ConstSpan<Plaintext> b) const {
@@ -463,7 +485,7 @@ class Evaluator {
     const auto x = detail::CtLimbs(pk_, a), y = detail::CtLimbs(pk_, b);
     std::vector<uint32_t> out(x.size());
     detail::Check(hg_sub(ctx(), id(), x.data(), y.data(), out.data(), a.size()));
-    return detail::ToCts(out, pk_.Limbs());
+    return detail::ToCts(pk_, out);
   }
   std::vector<Ciphertext> Sub(ConstSpan<Ciphertext> a, ConstSpan<Plaintext> b) const {
     std::vector<Plaintext> neg(b.size());
@@ -518,7 +540,7 @@ class Evaluator {
       }
       detail::Check(hg_mul_bn(ctx(), id(), x.data(), mag.data(), neg.data(), kl, out.data(), a.size()));
     }
-    return detail::ToCts(out, pk_.Limbs());
+    return detail::ToCts(pk_, out);
   }
   std::vector<Ciphertext> Mul(ConstSpan<Plaintext> a, ConstSpan<Ciphertext> b) const { return Mul(b, a); }
   std::vector<Plaintext> Mul(ConstSpan<Plaintext> a, ConstSpan<Plaintext> b) const {
@@ -535,7 +557,7 @@ class Evaluator {
     const auto x = detail::CtLimbs(pk_, a);
     std::vector<uint32_t> out(x.size());
     detail::Check(hg_negate(ctx(), id(), x.data(), out.data(), a.size()));
-    return detail::ToCts(out, pk_.Limbs());
+    return detail::ToCts(pk_, out);
   }
   void NegateInplace(Span<Ciphertext> a) const { Assign(a, Negate(Const(a))); }
 
@@ -543,7 +565,7 @@ class Evaluator {
     const auto x = detail::CtLimbs(pk_, a);
     std::vector<uint32_t> out(pk_.Limbs());
     detail::Check(hg_sum(ctx(), id(), x.data(), a.size(), out.data()));
-    return detail::ToCts(out, pk_.Limbs())[0];
+    return detail::ToCts(pk_, out)[0];
   }
 
  private:

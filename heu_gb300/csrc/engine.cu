@@ -1386,6 +1386,36 @@ int hg_encrypt(hg_ctx* ctx, int key_id, const int64_t* m, const uint32_t* r, uin
   });
 }
 
+int hg_convert_radix(hg_ctx* ctx, int key_id, const uint32_t* in, uint32_t* out, size_t count, uint32_t radix_bits,
+                     int to_external) {
+  return guarded(__func__, [&] {
+    if (!in || !out) fail(HG_ERR_INVALID, "null argument");
+    HG_HOST_PROLOGUE
+    if (radix_bits == 0 || radix_bits > 65536) fail(HG_ERR_INVALID, "radix_bits must be in [1, 65536]");
+    // R = 2^(32 S) here, R_ext = 2^radix_bits there
+    const BN Rin = BN(1).shl(32 * (size_t)k->S) % k->N;
+    const BN Rext = BN(1).shl(radix_bits) % k->N;
+    // MM(c R, R_ext) = c R_ext;  MM(c R_ext, R^2 / R_ext) = c R
+    const BN K = to_external ? Rext : (((Rin * Rin) % k->N) * BN::invmod(Rext, k->N)) % k->N;
+    const std::vector<uint32_t> kl = K.limbs((size_t)k->S);
+    auto* dk = w.io[3].ensure<uint32_t>(cb);
+    h2d(dk, kl.data(), cb, w);
+    run_chunked(ctx, w, count, [&](Work& v, size_t off, size_t cnt) {
+      auto* di = v.io[0].ensure<uint32_t>(cnt * cb);
+      auto* dout = v.io[1].ensure<uint32_t>(cnt * cb);
+      uint32_t* kv = dk;
+      if (&v != &w) {  // the other lane needs its own copy of the constant
+        kv = v.io[3].ensure<uint32_t>(cb);
+        h2d(kv, kl.data(), cb, v);
+      }
+      h2d(di, (const uint8_t*)in + off * cb, cnt * cb, v);
+      cuda_check(hg::launch_mul_const(k->S, k->kc, di, kv, dout, cnt, v.errp(), v.stream), "radix launch");
+      d2h((uint8_t*)out + off * cb, dout, cnt * cb, v);
+    });
+    return HG_OK;
+  });
+}
+
 int hg_encrypt_encoded(hg_ctx* ctx, int key_id, int codec, int64_t scale, int padding_bits, const void* values,
                        const void* values2, const uint32_t* r, uint32_t* ct_out, size_t count) {
   return guarded(__func__, [&] {

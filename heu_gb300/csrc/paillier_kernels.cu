@@ -66,6 +66,24 @@ __global__ void __launch_bounds__(kBlock) k_convert(KeyConst kc, const uint32_t*
   convert_one<TPI, L>(kc, in, out, to_mont, i, active, N, g, err);
 }
 
+// out = MM(in, C) = in * C * R^-1 for one constant C (device memory): moves
+// Montgomery residues between radices (C = R_ext mod N to the radix R_ext,
+// R^2 * R_ext^-1 mod N back).
+template <int TPI, int L>
+__global__ void __launch_bounds__(kBlock) k_mul_const(KeyConst kc, const uint32_t* __restrict__ in,
+                                                      const uint32_t* __restrict__ c, uint32_t* __restrict__ out,
+                                                      size_t count, uint32_t* err) {
+  constexpr int S = TPI * L;
+  HG_INSTANCE_PROLOGUE(count)
+  uint32_t N[L], A[L], B[L];
+  load_slice<L>(N, kc.N + g.t * L);
+  load_slice<L>(A, in + i * S + g.t * L);
+  check_ct<TPI, L>(A, N, active, g, err);
+  load_slice<L>(B, c + g.t * L);
+  mont_mul<TPI, L>(A, A, B, N, kc.np, g);
+  if (active) store_slice<L>(out + i * S + g.t * L, A);
+}
+
 // Persistent: each instance slot of the grid owns an odd-power table.
 template <int TPI, int L>
 __global__ void __launch_bounds__(kBlock) k_mul(KeyConst kc, const uint32_t* __restrict__ a,
@@ -421,6 +439,13 @@ int resident_blocks_mul_bn(int S) {
 cudaError_t launch_sel_from_neg(const uint8_t* neg, int64_t* sel, size_t count, cudaStream_t st) {
   if (count == 0) return cudaSuccess;
   k_sel_from_neg<<<(unsigned)((count + 255) / 256), 256, 0, st>>>(neg, sel, count);
+  return counted();
+}
+
+cudaError_t launch_mul_const(int S, const KeyConst& kc, const uint32_t* in, const uint32_t* c, uint32_t* out,
+                             size_t count, uint32_t* err, cudaStream_t st) {
+  if (count == 0) return cudaSuccess;
+  HG_DISPATCH_S0(S, k_mul_const<TPI, L><<<blocks_for(count, TPI), kBlock, 0, st>>>(kc, in, c, out, count, err));
   return counted();
 }
 

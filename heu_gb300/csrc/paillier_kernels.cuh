@@ -131,6 +131,9 @@ cudaError_t launch_ou_split_i64(const int64_t* p, int negate, uint32_t* ep, uint
                                 cudaStream_t st);
 cudaError_t launch_ou_split_mag(const uint32_t* mag, const uint8_t* neg, int limbs, const uint32_t* maxpt,
                                 uint32_t* ep, uint32_t* en, size_t count, uint32_t* err, cudaStream_t st);
+// out[i] = MM(in[i], c) with one S-limb constant c in device memory
+cudaError_t launch_mul_const(int S, const KeyConst& kc, const uint32_t* in, const uint32_t* c, uint32_t* out,
+                             size_t count, uint32_t* err, cudaStream_t st);
 cudaError_t launch_convert(int S, const KeyConst& kc, const uint32_t* in, uint32_t* out, size_t count,
                            int to_mont, uint32_t* err, cudaStream_t st);
 cudaError_t launch_reduce(int S, const KeyConst& kc, const uint32_t* in, size_t count, int chunk,

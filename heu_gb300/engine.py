@@ -63,6 +63,29 @@ def keygen(key_bits, seed):
     }
 
 
+def backend_radix_bits(n2_bits, backend):
+    """Montgomery radix exponent of a yacl BigInt backend for a modulus of
+    n2_bits bits: OpenSSL's BN_MONT_CTX and GMP use 64-bit limbs (R =
+    2^(64 * ceil(bits / 64))), libtommath 60-bit digits (R = 2^(60 *
+    ceil(bits / 60)))."""
+    if backend in ("openssl", "gmp"):
+        return 64 * -(-n2_bits // 64)
+    if backend == "tommath":
+        return 60 * -(-n2_bits // 60)
+    raise ValueError("backend must be openssl, gmp or tommath")
+
+
+def radix_constant(n2, limbs, radix_bits, to_external):
+    """The constant C with MM(c * R, C) = c * R_ext (to_external) or
+    MM(c * R_ext, C) = c * R mod n2, R = 2^(32 * limbs), R_ext = 2^radix_bits,
+    MM(x, y) = x * y * R^-1 mod n2."""
+    r_in = pow(2, 32 * limbs, n2)
+    r_ext = pow(2, radix_bits, n2)
+    if to_external:
+        return r_ext  # MM(c R, R_ext) = c R_ext
+    return r_in * r_in * pow(r_ext, -1, n2) % n2  # MM(c R_ext, R^2 / R_ext) = c R
+
+
 def ou_sizes(key_bits):
     """(ciphertext limbs S, secret limbs S/2) of an OU key."""
     if key_bits == 1024:
@@ -230,6 +253,14 @@ class Key:
         capi.check(self.lib.hg_decrypt_decoded(self.ctx.handle, self.id, codec, int(scale), int(padding_bits),
                                                _ptr(ct), _ptr(out), _ptr(out2), _ptr(ovf), n))
         return (out, out2, ovf) if batch else (out, ovf)
+
+    def convert_radix(self, ct, radix_bits, to_external):
+        """c * R <-> c * 2^radix_bits mod n^2 (hg_convert_radix)."""
+        ct = self._ct(ct)
+        out = self._out(ct.shape[0])
+        capi.check(self.lib.hg_convert_radix(self.ctx.handle, self.id, _ptr(ct), _ptr(out), ct.shape[0],
+                                             int(radix_bits), 1 if to_external else 0))
+        return out
 
     def encrypt_zero(self, r):
         r = _u32(r).reshape(-1, self.r_limbs)

@@ -121,6 +121,17 @@ int hg_randomize(hg_ctx* ctx, int key_id, uint32_t* ct, const uint32_t* r, size_
 int hg_decrypt(hg_ctx* ctx, int key_id, const uint32_t* ct, int64_t* m_out, uint8_t* overflow, size_t count);
 int hg_decrypt_bn(hg_ctx* ctx, int key_id, const uint32_t* ct, uint32_t* m_mag, uint8_t* m_neg, size_t count);
 
+/* Montgomery radix at the boundary.  Ciphertexts here are c * R mod n^2
+ * with R = 2^(32 S) (S = 32-bit limbs of n^2), which is the radix of a
+ * yacl BigInt backend with 32- or 64-bit limbs (OpenSSL, GMP: R =
+ * 2^(64 * ceil(bits(n^2) / 64)), the same for key sizes that are multiples
+ * of 64 bits).  A HEU build whose backend uses another radix (libtommath's
+ * 60-bit digits: R = 2^(60 * ceil(bits(n^2) / 60))) converts its
+ * ciphertexts with this call: to_external = 1 maps c * R to c * 2^radix_bits
+ * mod n^2, 0 maps back (one Montgomery multiplication by a constant). */
+int hg_convert_radix(hg_ctx* ctx, int key_id, const uint32_t* in, uint32_t* out, size_t count, uint32_t radix_bits,
+                     int to_external);
+
 /* ---- plaintext encodings on the device ----------------------------------
  * HEU's PlainEncoder (phe/encoding/plain_encoder.h:46-74, pylib's
  * IntegerEncoder / FloatEncoder) and BatchEncoder (phe/encoding/

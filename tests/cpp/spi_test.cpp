@@ -190,6 +190,25 @@ int main(int argc, char** argv) {
   EXPECT(dec.Decrypt(hea::ConstSpan<pg::Ciphertext>(std::vector<const pg::Ciphertext*>{&rs}))[0] ==
          a[0] + a[1] + a[2] + a[3]);
 
+  // a HEU build whose yacl backend keeps Montgomery residues in another
+  // radix (libtommath: 60-bit digits) exchanges ciphertexts in that radix
+  pg::PublicKey pk60 = pk;
+  const size_t radix60 = 60 * ((pk.n_square_.BitCount() + 59) / 60);
+  pk60.SetBackendRadixBits(radix60);
+  pg::Encryptor enc60(pk60);
+  pg::Decryptor dec60(pk60, sk);
+  pg::Evaluator ev60(pk60);
+  auto c60 = enc60.Encrypt(PA);
+  print_cts("radix60", c60);
+  std::printf("radix60_bits %zu\n", radix60);
+  auto d60 = dec60.Decrypt(hea::ConstSpan<pg::Ciphertext>(ptrs(c60)));
+  auto s60 = dec60.Decrypt(hea::ConstSpan<pg::Ciphertext>(ptrs(ev60.Add(hea::ConstSpan<pg::Ciphertext>(ptrs(c60)),
+                                                                           hea::ConstSpan<pg::Ciphertext>(ptrs(c60))))));
+  for (size_t i = 0; i < a.size(); ++i) {
+    EXPECT(d60[i] == a[i]);
+    EXPECT(s60[i] == a[i] + a[i]);
+  }
+
   // scalars wider than int64 (evaluator.cc:99-123 takes any BigInt)
   std::vector<pg::Plaintext> wide = {half, -half, pg::BigInt(1) - half, pg::BigInt::FromHex("10000000000000000")};
   auto mul_big = ev.Mul(A, hea::ConstSpan<pg::Plaintext>(ptrs(wide)));

@@ -45,6 +45,11 @@ def test_cpp_spi_matches_oracle(bits):
         assert int(got[f"mul_cp[{i}]"], 16) == mont(pz.mul(pk, ca[i], b[i]))
         assert int(got[f"neg[{i}]"], 16) == mont(pz.negate(pk, ca[i]))
     assert int(got["sum"], 16) == mont(pz.sum_(pk, ca))
+    e60 = int(got["radix60_bits"])
+    assert e60 == 60 * -(-pk.n2.bit_length() // 60)
+    for i in range(len(a)):
+        z = int(got[f"radix60[{i}]"], 16) * pow(2, -e60, pk.n2) % pk.n2
+        assert pz.decrypt(pk, sk, z) == a[i], f"radix60[{i}]"
     wide = [half, -half, 1 - half, 2 ** 64]
     for i, kv in enumerate(wide):
         assert int(got[f"mul_big[{i}]"], 16) == mont(pz.mul(pk, ca[i], kv)), f"mul_big[{i}]"

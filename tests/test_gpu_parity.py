@@ -332,6 +332,20 @@ def test_montgomery_conversion_roundtrip(kk):
     assert hg.limbs_to_ints(key.from_mont(mont)) == zs
 
 
+@pytest.mark.parametrize("backend", ["openssl", "tommath"])
+def test_backend_radix_conversion(kk, backend):
+    """hg_convert_radix: c * R <-> c * R_ext for a yacl backend's radix."""
+    from heu_gb300.engine import backend_radix_bits
+
+    key, pk, sk = kk
+    e = backend_radix_bits(pk.n2.bit_length(), backend)
+    zs = [pz.encrypt(pk, m, r) for m, r in zip([0, 7, -9, 2 ** 50], pz.r_stream(31, 4, pk.key_size // 2))]
+    ours = to_mont_limbs(pk, key, zs)
+    ext = key.convert_radix(ours, e, True)
+    assert hg.limbs_to_ints(ext) == [z * pow(2, e, pk.n2) % pk.n2 for z in zs]
+    assert np.array_equal(key.convert_radix(ext, e, False), ours)
+
+
 def test_table_window_does_not_change_results(gpu_ctx):
     pk, sk = pz.keygen(1024, 1)
     ms = [1, -2, 3, 2 ** 40]

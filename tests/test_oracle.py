@@ -275,3 +275,33 @@ def test_c_restatement_reductions_match_python_oracle():
     cx = [[zs[i * 8 + j] for j in range(8)] for i in range(6)]
     assert [pz.from_mont(pk, v) for v in ck.ints(out.reshape(-1, ck.s))] == \
         [v for row in pz.matmul(pk, cx, y.tolist()) for v in row]
+
+
+@pytest.mark.parametrize("bits,seed", [(1024, 1), (2048, 0)])
+@pytest.mark.parametrize("backend", ["openssl", "gmp", "tommath"])
+def test_montgomery_radix_conversion(bits, seed, backend):
+    """Ciphertexts move between this engine's radix R = 2^(32 S) and a yacl
+    backend's: one Montgomery multiplication by radix_constant each way,
+    checked with Python integers (the same constants hg_convert_radix
+    computes)."""
+    from heu_gb300.engine import backend_radix_bits, radix_constant
+
+    pk, sk = oracle_key(bits, seed)
+    n2 = pk.n2
+    S = bits // 16
+    e = backend_radix_bits(n2.bit_length(), backend)
+    if backend in ("openssl", "gmp"):
+        assert e == 32 * S  # same radix as this engine for these key sizes
+    else:
+        assert e == 60 * -(-n2.bit_length() // 60) and e != 32 * S
+    r_inv = pow(2 ** (32 * S), -1, n2)
+
+    def mm(x, y):
+        return x * y * r_inv % n2
+
+    zs = [pz.encrypt(pk, m, r) for m, r in zip([0, 1, -5, 2 ** 40], pz.r_stream(30, 4, pk.key_size // 2))]
+    for z in zs:
+        ours = pz.to_mont(pk, z)
+        theirs = mm(ours, radix_constant(n2, S, e, True))
+        assert theirs == z * pow(2, e, n2) % n2
+        assert mm(theirs, radix_constant(n2, S, e, False)) == ours
