@@ -669,6 +669,7 @@ def c4_measure(args, steps, warmup):
         base = torch.empty((n, S), dtype=torch.int32, device=dev)
         capi.check(lib.hg_dev_encrypt(h, key.id, ctypes.c_void_p(m.data_ptr()), ctypes.c_void_p(r.data_ptr()),
                                       ctypes.c_void_p(base.data_ptr()), n, None))
+        torch.cuda.synchronize()  # torch's stream reads `base` below; the engine's stream wrote it
         j = dict(key=key, n=n, op=op, m=m, r=r, base=base)
         if op == MUL:
             j["k"] = torch.randint(-(2 ** 63), 2 ** 63 - 1, (n,), dtype=torch.int64, device=dev, generator=gen)
@@ -803,6 +804,7 @@ def c3_measure(args, steps, warmup):
         return ctypes.c_void_p(t.data_ptr())
 
     capi.check(lib.hg_dev_encrypt(h, key.id, P(g), P(r), P(ct), n, None))
+    torch.cuda.synchronize()  # the reductions below run on another stream
     om = torch.from_numpy(rng.integers(0, B, size=(n, F)).astype(np.uint8)).to(dev)
     bsum = torch.empty((F * B, key.ct_limbs), dtype=torch.int32, device=dev)
     s1 = torch.empty((1, key.ct_limbs), dtype=torch.int32, device=dev)
@@ -1190,7 +1192,7 @@ def c5_measure(args, rates, nreq_for_rate):
 
     server = hg.Server(ctx, budget_bytes=40 << 30, slots=args.slots, max_batch_elems=1 << 18,
                        batch_us=args.batch_us, slice_us=args.slice_us, policy=args.policy,
-                       express_us=args.express_us, express_len=args.express_len)
+                       express_us=args.express_us, express_len=args.express_len, express_share=args.express_share)
     for key in keys:
         m = torch.randint(-(2 ** 40), 2 ** 40, (LMAX,), dtype=torch.int64, device=dev, generator=gen)
         r = torch.randint(-(2 ** 31), 2 ** 31, (LMAX, key.r_limbs), dtype=torch.int32, device=dev, generator=gen)
@@ -1295,6 +1297,7 @@ def c5_measure(args, rates, nreq_for_rate):
                    "policy": ["shortest-remaining-first", "fifo"][args.policy],
                    "express_us": args.express_us if args.express_us > 0 else None,
                    "express_len": args.express_len or None,
+                   "express_share": args.express_share or None,
                    "capacity_note": "mean request = (65536-1)/ln(65536) = 5,909 elements, so rates above "
                                     "~200 req/s offer more elements/s than one GB300 serves; lower rates are "
                                     "sub-capacity"},
@@ -1329,6 +1332,8 @@ def main():
     ap.add_argument("--batch-us", type=float, default=0.0, help="config5: server micro-batch target (0 = default)")
     ap.add_argument("--slice-us", type=float, default=0.0, help="config5: server slice per request (0 = default)")
     ap.add_argument("--slots", type=int, default=5, help="config5: concurrent micro-batches")
+    ap.add_argument("--express-share", type=float, default=0.0,
+                    help="config5: share of every SM's batch blocks kept for the express slots (0 = default)")
     ap.add_argument("--express-len", type=int, default=1024,
                     help="config5: requests of at most this many elements run in the latency class (0 = off)")
     ap.add_argument("--no-extras", action="store_true",

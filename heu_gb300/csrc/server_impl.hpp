@@ -361,11 +361,13 @@ void scheduler(hg_server* sp) {
     if (s.express_us >= 0.0)
       for (const Req* q : s.pending)
         if (klass(q) != 0) short_backlog += elem_cost_us(*q->k, q->r.op) * (double)(q->r.count - q->next);
-    // an express batch of the length rule holds up to 4 short requests'
-    // worth of elements; of the cost rule, 4 x express_us of work
+    // an express batch of the length rule holds at most express_len
+    // elements (one longest short request, or several shorter ones; a batch
+    // lasts as long as its slowest chain, so small batches keep the tail
+    // short); of the cost rule, 4 x express_us of work
     const double express_batch_us =
         s.express_len > 0 ? 1e300 : 4.0 * std::max(s.express_us, 1.0);
-    const size_t express_batch_elems = s.express_len > 0 ? 4 * s.express_len : s.cfg.max_batch_elems;
+    const size_t express_batch_elems = s.express_len > 0 ? s.express_len : s.cfg.max_batch_elems;
     for (auto& slp : s.slots) {
       Slot& sl = *slp;
       if (sl.busy || s.pending.empty()) continue;
