@@ -24,6 +24,10 @@ __global__ void __launch_bounds__(kBlock) k_decrypt(KeyConst kc, SecConst sc, co
   constexpr int UPW = 32 / (2 * TP);  // ciphertexts per warp
   constexpr int UPB = kBlock / (2 * TP);
   __shared__ __align__(16) uint32_t ysm[UPB][2 * SP];
+  // squaring scratch per warp (mont_sqr); layouts whose scratch would push
+  // the block past 48 KB of static shared memory square with mont_mul
+  constexpr bool kSqr = LP <= 16;
+  __shared__ __align__(16) uint32_t sqr_smem[kBlock / 32][kSqr ? sqr_smem_words<LP>() : 1];
   const Group<TP> g;
   const int lane = threadIdx.x & 31;
   const int side = (lane / TP) & 1;
@@ -35,7 +39,7 @@ __global__ void __launch_bounds__(kBlock) k_decrypt(KeyConst kc, SecConst sc, co
     const size_t inst = wbase + unit_w;
     const bool active = inst < count;
     decrypt_one<TP, LP>(kc, sc, ct, active ? inst : count - 1, active, side, tb, ysm[unit_b], out_i64, out_ovf,
-                        out_mag, out_neg, g, err, cd);
+                        out_mag, out_neg, g, err, cd, kSqr ? sqr_smem[threadIdx.x >> 5] : nullptr);
   }
 }
 
@@ -62,8 +66,8 @@ int resident_blocks_decrypt(int Sp, int variant) {
   return r;
 }
 
-// Ciphertexts of one wave of the latency layout (a half warp per CRT side,
-// one ciphertext per warp); batches up to this size run in that layout.
+// Batches up to one wave of the latency layout (a half warp per CRT side,
+// one ciphertext per warp), and at most 12 per SM, run in that layout.
 static size_t latency_wave_decrypt(int Sp) {
   static size_t cache[3] = {0, 0, 0};
   const int slot = Sp == 32 ? 0 : Sp == 64 ? 1 : 2;
@@ -71,6 +75,13 @@ static size_t latency_wave_decrypt(int Sp) {
     size_t v = 0;
     [&]() -> cudaError_t {
       HG_DISPATCH_SPL(Sp, v = (size_t)occupancy_blocks(k_decrypt<TP, LP>) * (kBlock / 32));
+      int dev = 0, sms = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      // at most 12 ciphertexts per SM (4096 took 18.3 ms in this layout
+      // against 16.1 ms in the throughput layout on GB300, one 4.2 ms
+      // against 10.2 ms)
+      v = std::min(v, (size_t)12 * (size_t)sms);
       return cudaSuccess;
     }();
     cache[slot] = v;

@@ -2687,7 +2687,9 @@ int hg_server_create(hg_ctx* ctx, const hg_server_config* cfg, hg_server** out) 
     s->express_us = (cfg && cfg->express_us != 0.0) ? cfg->express_us : -1.0;
     s->express_len = cfg ? cfg->express_len : 0;
     if (s->express_len > 0) s->express_us = 0.0;  // the length rule replaces the cost rule
-    const double share = (cfg && cfg->express_share > 0.0) ? cfg->express_share : 0.25;
+    // the length rule's two express slots keep half of every SM's blocks (one
+    // each at four per SM); the cost rule's one slot a quarter
+    const double share = (cfg && cfg->express_share > 0.0) ? cfg->express_share : s->express_len > 0 ? 0.5 : 0.25;
     if (share >= 1.0) fail(HG_ERR_INVALID, "express_share must be below 1");
     if (c.slots < 2 || bps < 2) {
       s->express_us = -1.0;
@@ -2737,7 +2739,12 @@ int hg_server_create(hg_ctx* ctx, const hg_server_config* cfg, hg_server** out) 
       s->slots.push_back(std::move(sl));
     }
     hg_server* raw = s.get();
-    s->sched = std::thread(scheduler, raw);
+    if (s->express_len > 0) {
+      s->sched = std::thread(scheduler, raw, 0);
+      s->sched_express = std::thread(scheduler, raw, 1);
+    } else {
+      s->sched = std::thread(scheduler, raw, -1);
+    }
     *out = s.release();
     return HG_OK;
   });
@@ -2752,6 +2759,7 @@ int hg_server_destroy(hg_server* s) {
     }
     s->cv_work.notify_all();
     if (s->sched.joinable()) s->sched.join();
+    if (s->sched_express.joinable()) s->sched_express.join();
     cudaSetDevice(s->ctx->device);
     for (auto& sl : s->slots) {
       cudaStreamSynchronize(sl->st);
@@ -2821,7 +2829,7 @@ int hg_server_submit(hg_server* s, const hg_request* req, uint64_t* ticket) {
       s->pending.push_back(q.get());
       s->reqs[q->id] = std::move(q);
     }
-    s->cv_work.notify_one();
+    s->cv_work.notify_all();
     return HG_OK;
   });
 }

@@ -323,13 +323,20 @@ int instances_per_block(int S, int variant) {
   return kBlock / tpi;
 }
 
-// Instances of one wave of a latency-layout kernel (one instance per warp):
-// batches up to this size run in that layout, since they leave the GPU
-// mostly idle in the throughput layout and finish sooner with fewer limbs
-// per lane on each dependent chain.
+// Batches up to this size run in the latency layout (one instance per
+// warp): they leave the GPU mostly idle in the throughput layout and finish
+// sooner with fewer limbs per lane on each dependent chain.  The bound is
+// one wave of the latency layout, and at most 12 instances per SM: beyond
+// that the latency layout's lower efficiency per multiplication (more
+// shuffles per limb) costs more than its shorter chains save (measured on
+// GB300: 4096 encryptions took 1.66 ms in the latency layout against
+// 1.47 ms in the throughput layout, one took 0.38 ms against 0.91 ms).
 template <typename K>
 static size_t latency_wave(K kernel) {
-  return (size_t)occupancy_blocks(kernel) * (kBlock / 32);
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return std::min((size_t)occupancy_blocks(kernel) * (kBlock / 32), (size_t)12 * (size_t)sms);
 }
 
 static size_t latency_wave_encrypt(int S) {

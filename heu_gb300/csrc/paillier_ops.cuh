@@ -8,6 +8,7 @@
 // and ballots inside).
 #pragma once
 #include "mont.cuh"
+#include "mont_sqr.cuh"
 #include "paillier_kernels.cuh"
 
 namespace hg {
@@ -685,7 +686,7 @@ __device__ __forceinline__ void decrypt_one(const KeyConst& kc, const SecConst& 
                                             uint32_t* ysm, int64_t* __restrict__ out_i64,
                                             uint8_t* __restrict__ out_ovf, uint32_t* __restrict__ out_mag,
                                             uint8_t* __restrict__ out_neg, const Group<TP>& g, uint32_t* err,
-                                            const Codec& cd = Codec{}) {
+                                            const Codec& cd = Codec{}, uint32_t* sqr_smem = nullptr) {
   constexpr int SP = TP * LP;
   const int ntab = 1 << (sc.wd - 1);
   uint32_t N[LP];
@@ -711,7 +712,10 @@ __device__ __forceinline__ void decrypt_one(const KeyConst& kc, const SecConst& 
   mont_redc_wide<TP, LP>(x, lo, hi, N, np, g);
   store_slice<LP>(tb, x);
   uint32_t x2[LP], cur[LP];
-  mont_mul<TP, LP>(x2, x, x, N, np, g);
+  if (sqr_smem)
+    mont_sqr<TP, LP>(x2, x, N, np, g, sqr_smem);
+  else
+    mont_mul<TP, LP>(x2, x, x, N, np, g);
   copy_slice<LP>(cur, x);
 #pragma unroll 1
   for (int t = 1; t < ntab; ++t) {
@@ -723,6 +727,12 @@ __device__ __forceinline__ void decrypt_one(const KeyConst& kc, const SecConst& 
 #pragma unroll 1
   for (int s = 0; s < sc.prog_len; ++s) {
     const uint16_t op = prog[s];
+    // the two CRT sides follow different programs in one warp: a step where
+    // both square runs the squaring, any other step one multiplication
+    if (sqr_smem && __all_sync(kFull, op == kOpSquare)) {
+      mont_sqr<TP, LP>(acc, acc, N, np, g, sqr_smem);
+      continue;
+    }
     uint32_t B[LP];
     if (op < kOpNop) {
       load_slice<LP>(B, tb + (size_t)op * SP);

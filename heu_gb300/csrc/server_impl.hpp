@@ -124,6 +124,7 @@ struct hg_server {
   size_t regular_smem = 0;     // dynamic shared memory that keeps regular batches
                                // off the express slot's blocks on every SM
   std::thread sched;
+  std::thread sched_express;  // the express slots' scheduler (length rule)
 };
 
 namespace {
@@ -302,7 +303,29 @@ void finish_req(hg_server& s, Req* q) {
   s.cv_done.notify_all();
 }
 
-void scheduler(hg_server* sp) {
+// Class of a pending request: 0 regular, 1 express, 2 express decrypt.
+// With express_len, short = at most express_len elements (short
+// decryptions get their own express slot when there is one); otherwise
+// short = estimated remaining work <= express_us.
+int req_class(const hg_server& s, const Req* q) {
+  if (s.express_len > 0) {
+    if (q->r.count > s.express_len) return 0;
+    bool dec_slot = false;
+    for (auto& slp : s.slots) dec_slot |= slp->express_dec;
+    return (dec_slot && q->r.op == hg::kBatchDecrypt) ? 2 : 1;
+  }
+  if (s.express_us < 0.0) return 0;
+  const double rem = elem_cost_us(*q->k, q->r.op) * (double)(q->r.count - q->next);
+  return rem <= s.express_us ? 1 : 0;
+}
+
+// One scheduler thread serves the regular slots (which = 0) and, with the
+// length rule, another one the express slots (which = 1), so short requests
+// are staged and launched without waiting for the host work (staging,
+// planning) of a long batch; which = -1 serves every slot.
+bool serves(const Slot& sl, int which) { return which < 0 || sl.express == (which == 1); }
+
+void scheduler(hg_server* sp, int which) {
   hg_server& s = *sp;
   cudaSetDevice(s.ctx->device);
   std::unique_lock<std::mutex> lk(s.mu);
@@ -310,7 +333,7 @@ void scheduler(hg_server* sp) {
     // retire finished slots
     for (auto& slp : s.slots) {
       Slot& sl = *slp;
-      if (!sl.busy) continue;
+      if (!sl.busy || !serves(sl, which)) continue;
       if (cudaEventQuery(sl.ev) != cudaSuccess) continue;
       const uint32_t bits = *sl.err_host;
       for (Slice& sc : sl.slices) {
@@ -326,7 +349,7 @@ void scheduler(hg_server* sp) {
     }
     if (s.stop && s.pending.empty()) {
       bool any = false;
-      for (auto& slp : s.slots) any |= slp->busy;
+      for (auto& slp : s.slots) any |= slp->busy && serves(*slp, which);
       if (!any) break;
     }
     // admit: every pending request gets a slice of at most slice_us of work
@@ -340,21 +363,7 @@ void scheduler(hg_server* sp) {
         return ra < rb;
       });
     bool launched = false;
-    // class of a pending request: 0 regular, 1 express, 2 express decrypt.
-    // With express_len, short = at most express_len elements (short
-    // decryptions get their own express slot when there is one); otherwise
-    // short = estimated remaining work <= express_us.
-    bool dec_slot = false;
-    for (auto& slp : s.slots) dec_slot |= slp->express_dec;
-    auto klass = [&](const Req* q) -> int {
-      if (s.express_len > 0) {
-        if (q->r.count > s.express_len) return 0;
-        return (dec_slot && q->r.op == hg::kBatchDecrypt) ? 2 : 1;
-      }
-      if (s.express_us < 0.0) return 0;
-      const double rem = elem_cost_us(*q->k, q->r.op) * (double)(q->r.count - q->next);
-      return rem <= s.express_us ? 1 : 0;
-    };
+    auto klass = [&](const Req* q) -> int { return req_class(s, q); };
     // short requests belong to the express slots unless their backlog
     // exceeds what those take per batch
     double short_backlog = 0.0;
@@ -370,7 +379,7 @@ void scheduler(hg_server* sp) {
     const size_t express_batch_elems = s.express_len > 0 ? s.express_len : s.cfg.max_batch_elems;
     for (auto& slp : s.slots) {
       Slot& sl = *slp;
-      if (sl.busy || s.pending.empty()) continue;
+      if (sl.busy || s.pending.empty() || !serves(sl, which)) continue;
       size_t elems = 0, bytes = 0;
       double cost = 0.0;
       const double batch_cap = sl.express ? express_batch_us : s.batch_us;
@@ -456,12 +465,20 @@ void scheduler(hg_server* sp) {
     }
     if (!launched) {
       bool any_busy = false;
-      for (auto& slp : s.slots) any_busy |= slp->busy;
-      // poll busy slots quickly; sleep when idle until work arrives
+      for (auto& slp : s.slots) any_busy |= slp->busy && serves(*slp, which);
+      // poll busy slots quickly; sleep when idle until work of this thread's
+      // slots arrives (with the length rule each thread waits for its class)
+      auto mine = [&] {
+        if (s.stop) return true;
+        if (which < 0 || s.express_len == 0) return !s.pending.empty();
+        for (const Req* q : s.pending)
+          if ((req_class(s, q) != 0) == (which == 1)) return true;
+        return false;
+      };
       if (any_busy)
         s.cv_work.wait_for(lk, std::chrono::microseconds(20));
       else
-        s.cv_work.wait_for(lk, std::chrono::milliseconds(5), [&] { return s.stop || !s.pending.empty(); });
+        s.cv_work.wait_for(lk, std::chrono::milliseconds(5), mine);
     }
   }
 }

@@ -287,7 +287,8 @@ typedef struct {
                              batches then run on the remaining share
                              (0 or < 0 = no express slot; needs slots >= 2) */
   double express_share;   /* share of every SM's batch-kernel blocks kept for
-                             the express slot (0 = 0.25, i.e. 1 of 4) */
+                             the express slots (0 = 0.5 with express_len,
+                             0.25 with express_us) */
   size_t express_len;     /* > 0: latency class by length instead of
                              express_us: requests of at most this many
                              elements run in the express slots, in the
@@ -295,7 +296,9 @@ typedef struct {
                              ciphertext), each batch as soon as a slot is
                              free; with slots >= 3 short decryptions get an
                              express slot of their own (slot 1), so the
-                             other short requests never wait for a CRT chain */
+                             other short requests never wait for a CRT chain;
+                             a scheduler thread of their own stages and
+                             launches the express batches */
 } hg_server_config;
 #define HG_POLICY_SHORTEST 0
 #define HG_POLICY_FIFO 1
