@@ -250,7 +250,7 @@ template <int TPI, int L>
 __device__ __forceinline__ void mul_one(const KeyConst& kc, const uint32_t* __restrict__ a,
                                         const int64_t* __restrict__ kk, uint32_t* __restrict__ out, size_t i,
                                         bool active, uint32_t* __restrict__ tb, int wm, const uint32_t (&N)[L],
-                                        const Group<TPI>& g, uint32_t* err) {
+                                        const Group<TPI>& g, uint32_t* err, uint32_t* sqr_smem = nullptr) {
   constexpr int S = TPI * L;
   const int ntab = 1 << (wm - 1);
   const uint64_t e = abs_i64(kk[i]);
@@ -259,7 +259,10 @@ __device__ __forceinline__ void mul_one(const KeyConst& kc, const uint32_t* __re
   check_ct<TPI, L>(x, N, active, g, err);
   store_slice<L>(tb, x);
   uint32_t x2[L], cur[L];
-  mont_mul<TPI, L>(x2, x, x, N, kc.np, g);
+  if (sqr_smem)
+    mont_sqr<TPI, L>(x2, x, N, kc.np, g, sqr_smem);
+  else
+    mont_mul<TPI, L>(x2, x, x, N, kc.np, g);
   copy_slice<L>(cur, x);
 #pragma unroll 1
   for (int t = 1; t < ntab; ++t) {
@@ -301,6 +304,11 @@ __device__ __forceinline__ void mul_one(const KeyConst& kc, const uint32_t* __re
       }
     }
     if (!__any_sync(kFull, op != 0)) break;
+    // a step where every group of the warp squares runs as a squaring
+    if (sqr_smem && __all_sync(kFull, op == 1)) {
+      mont_sqr<TPI, L>(acc, acc, N, kc.np, g, sqr_smem);
+      continue;
+    }
     uint32_t B[L];
     if (op == 2) {
       load_slice<L>(B, tb + (size_t)mulidx * S);
