@@ -24,10 +24,6 @@ __global__ void __launch_bounds__(kBlock) k_decrypt(KeyConst kc, SecConst sc, co
   constexpr int UPW = 32 / (2 * TP);  // ciphertexts per warp
   constexpr int UPB = kBlock / (2 * TP);
   __shared__ __align__(16) uint32_t ysm[UPB][2 * SP];
-  // squaring scratch per warp (mont_sqr); layouts whose scratch would push
-  // the block past 48 KB of static shared memory square with mont_mul
-  constexpr bool kSqr = LP <= 16;
-  __shared__ __align__(16) uint32_t sqr_smem[kBlock / 32][kSqr ? sqr_smem_words<LP>() : 1];
   const Group<TP> g;
   const int lane = threadIdx.x & 31;
   const int side = (lane / TP) & 1;
@@ -39,7 +35,7 @@ __global__ void __launch_bounds__(kBlock) k_decrypt(KeyConst kc, SecConst sc, co
     const size_t inst = wbase + unit_w;
     const bool active = inst < count;
     decrypt_one<TP, LP>(kc, sc, ct, active ? inst : count - 1, active, side, tb, ysm[unit_b], out_i64, out_ovf,
-                        out_mag, out_neg, g, err, cd, kSqr ? sqr_smem[threadIdx.x >> 5] : nullptr);
+                        out_mag, out_neg, g, err, cd);
   }
 }
 

@@ -97,11 +97,6 @@ __global__ void __launch_bounds__(kBlock) k_ou_decrypt(KeyConst kc, OuConst oc, 
   constexpr int UPW = 32 / TP;
   constexpr int UPB = kBlock / TP;
   __shared__ __align__(16) uint32_t ysm[UPB][SP];
-  // squaring scratch per warp (mont_sqr): the exponent program is shared by
-  // every ciphertext, so each of its squaring steps runs as a squaring
-  constexpr bool kSqr = LP <= 16;
-  __shared__ __align__(16) uint32_t sqr_smem[kBlock / 32][kSqr ? sqr_smem_words<LP>() : 1];
-  uint32_t* sq = kSqr ? sqr_smem[threadIdx.x >> 5] : nullptr;
   const Group<TP> g;
   const int lane = threadIdx.x & 31;
   const int unit_w = lane / TP;
@@ -145,10 +140,7 @@ __global__ void __launch_bounds__(kBlock) k_ou_decrypt(KeyConst kc, OuConst oc, 
     mont_mul<TP, LP>(x, x, K, N, oc.np2, g);
     store_slice<LP>(tb, x);
     uint32_t x2[LP], cur[LP];
-    if (kSqr)
-      mont_sqr<TP, LP>(x2, x, N, oc.np2, g, sq);
-    else
-      mont_mul<TP, LP>(x2, x, x, N, oc.np2, g);
+    mont_mul<TP, LP>(x2, x, x, N, oc.np2, g);
     copy_slice<LP>(cur, x);
 #pragma unroll 1
     for (int t = 1; t < ntab; ++t) {
@@ -160,10 +152,6 @@ __global__ void __launch_bounds__(kBlock) k_ou_decrypt(KeyConst kc, OuConst oc, 
 #pragma unroll 1
     for (int s = 0; s < oc.prog_len; ++s) {
       const uint16_t op = oc.prog[s];
-      if (kSqr && op == kOpSquare) {
-        mont_sqr<TP, LP>(acc, acc, N, oc.np2, g, sq);
-        continue;
-      }
       uint32_t B[LP];
       if (op < kOpNop) {
         load_slice<LP>(B, tb + (size_t)op * SP);

@@ -98,16 +98,12 @@ __global__ void __launch_bounds__(kBlock) k_mul(KeyConst kc, const uint32_t* __r
   const int warp_first = (threadIdx.x >> 5) * IPW;
   const int ntab = 1 << (wm - 1);
   uint32_t* tb = scratch + ((size_t)blockIdx.x * IPB + warp_first + lane_inst) * (size_t)ntab * S + g.t * L;
-  // squaring scratch per warp (mont_sqr) for the throughput layouts
-  constexpr bool kSqr = TPI <= 8 && L <= 16;
-  __shared__ __align__(16) uint32_t sqr_smem[kBlock / 32][kSqr ? sqr_smem_words<L>() : 1];
   uint32_t N[L];
   load_slice<L>(N, kc.N + g.t * L);
   for (size_t wbase = next_work(ctr, IPW); wbase < count; wbase = next_work(ctr, IPW)) {
     const size_t inst = wbase + lane_inst;
     const bool active = inst < count;
-    mul_one<TPI, L>(kc, a, kk, out, active ? inst : count - 1, active, tb, wm, N, g, err,
-                    kSqr ? sqr_smem[threadIdx.x >> 5] : nullptr);
+    mul_one<TPI, L>(kc, a, kk, out, active ? inst : count - 1, active, tb, wm, N, g, err);
   }
 }
 

@@ -8,7 +8,6 @@
 // and ballots inside).
 #pragma once
 #include "mont.cuh"
-#include "mont_sqr.cuh"
 #include "paillier_kernels.cuh"
 
 namespace hg {
@@ -250,7 +249,7 @@ template <int TPI, int L>
 __device__ __forceinline__ void mul_one(const KeyConst& kc, const uint32_t* __restrict__ a,
                                         const int64_t* __restrict__ kk, uint32_t* __restrict__ out, size_t i,
                                         bool active, uint32_t* __restrict__ tb, int wm, const uint32_t (&N)[L],
-                                        const Group<TPI>& g, uint32_t* err, uint32_t* sqr_smem = nullptr) {
+                                        const Group<TPI>& g, uint32_t* err) {
   constexpr int S = TPI * L;
   const int ntab = 1 << (wm - 1);
   const uint64_t e = abs_i64(kk[i]);
@@ -259,10 +258,7 @@ __device__ __forceinline__ void mul_one(const KeyConst& kc, const uint32_t* __re
   check_ct<TPI, L>(x, N, active, g, err);
   store_slice<L>(tb, x);
   uint32_t x2[L], cur[L];
-  if (sqr_smem)
-    mont_sqr<TPI, L>(x2, x, N, kc.np, g, sqr_smem);
-  else
-    mont_mul<TPI, L>(x2, x, x, N, kc.np, g);
+  mont_mul<TPI, L>(x2, x, x, N, kc.np, g);
   copy_slice<L>(cur, x);
 #pragma unroll 1
   for (int t = 1; t < ntab; ++t) {
@@ -304,11 +300,6 @@ __device__ __forceinline__ void mul_one(const KeyConst& kc, const uint32_t* __re
       }
     }
     if (!__any_sync(kFull, op != 0)) break;
-    // a step where every group of the warp squares runs as a squaring
-    if (sqr_smem && __all_sync(kFull, op == 1)) {
-      mont_sqr<TPI, L>(acc, acc, N, kc.np, g, sqr_smem);
-      continue;
-    }
     uint32_t B[L];
     if (op == 2) {
       load_slice<L>(B, tb + (size_t)mulidx * S);
@@ -694,7 +685,7 @@ __device__ __forceinline__ void decrypt_one(const KeyConst& kc, const SecConst& 
                                             uint32_t* ysm, int64_t* __restrict__ out_i64,
                                             uint8_t* __restrict__ out_ovf, uint32_t* __restrict__ out_mag,
                                             uint8_t* __restrict__ out_neg, const Group<TP>& g, uint32_t* err,
-                                            const Codec& cd = Codec{}, uint32_t* sqr_smem = nullptr) {
+                                            const Codec& cd = Codec{}) {
   constexpr int SP = TP * LP;
   const int ntab = 1 << (sc.wd - 1);
   uint32_t N[LP];
@@ -720,10 +711,7 @@ __device__ __forceinline__ void decrypt_one(const KeyConst& kc, const SecConst& 
   mont_redc_wide<TP, LP>(x, lo, hi, N, np, g);
   store_slice<LP>(tb, x);
   uint32_t x2[LP], cur[LP];
-  if (sqr_smem)
-    mont_sqr<TP, LP>(x2, x, N, np, g, sqr_smem);
-  else
-    mont_mul<TP, LP>(x2, x, x, N, np, g);
+  mont_mul<TP, LP>(x2, x, x, N, np, g);
   copy_slice<LP>(cur, x);
 #pragma unroll 1
   for (int t = 1; t < ntab; ++t) {
@@ -735,12 +723,6 @@ __device__ __forceinline__ void decrypt_one(const KeyConst& kc, const SecConst& 
 #pragma unroll 1
   for (int s = 0; s < sc.prog_len; ++s) {
     const uint16_t op = prog[s];
-    // the two CRT sides follow different programs in one warp: a step where
-    // both square runs the squaring, any other step one multiplication
-    if (sqr_smem && __all_sync(kFull, op == kOpSquare)) {
-      mont_sqr<TP, LP>(acc, acc, N, np, g, sqr_smem);
-      continue;
-    }
     uint32_t B[LP];
     if (op < kOpNop) {
       load_slice<LP>(B, tb + (size_t)op * SP);

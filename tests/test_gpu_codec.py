@@ -46,7 +46,7 @@ def test_plain_i64_encode_matches_host_encoder(gpu_key, scale):
 def test_plain_f64_encode_and_decode_match_host_encoder(gpu_key):
     key, pk, sk = gpu_key(2048, 0)
     rng = np.random.default_rng(3)
-    edge = [0.0, -0.0, 1e-7, -1e-7, 0.5, -0.5, 1.5, -2.5, 2.0 ** 53 + 2, 1e30, -1e30, 1.7e300, -3.3e-300,
+    edge = [0.0, -0.0, 1e-7, -1e-7, 0.5, -0.5, 1.5, -2.5, 2.0 ** 53 + 2, 1e30, -1e30, 1.7e290, -3.3e-300,
             123.456789, -9.87654321e12]
     vals = np.array(edge + list(rng.standard_normal(200) * 1e3), dtype=np.float64)
     for scale in (1, 10 ** 6, 2 ** 40 + 7):
