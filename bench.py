@@ -1157,6 +1157,7 @@ def _latency_classes(lat, ops, lens, short_len):
 
     short = lens <= short_len
     out = {"short_le_%d" % short_len: pct(short),
+           "short_enc_add_sum": pct(short & ((ops == 0) | (ops == 2) | (ops == 4))),
            "short_non_decrypt": pct(short & (ops != 1)),
            "short_decrypt": pct(short & (ops == 1)),
            "long": pct(~short)}

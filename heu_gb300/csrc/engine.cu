@@ -526,7 +526,8 @@ void core_decrypt(KeyRec& k, Work& w, const uint32_t* ct, int64_t* m, uint8_t* o
 // out[i] = in[i]^-1 where sel == nullptr or sel[i] < 0, else in[i]; every
 // step is in stream order (graph-capturable).  `task` must outlive the work.
 void core_inverse_async_raw(KeyRec& k, const uint32_t* in, const int64_t* sel, uint32_t* out, size_t count,
-                            uint32_t* tr, InvTask& task, uint32_t* errp, cudaStream_t st);
+                            uint32_t* tr, InvTask& task, uint32_t* errp, cudaStream_t st,
+                            bool inline_host = false);
 
 void core_inverse_async(KeyRec& k, const uint32_t* in, const int64_t* sel, uint32_t* out, size_t count,
                         TreeBufs& tb, InvTask& task, uint32_t* errp, cudaStream_t st) {
@@ -538,9 +539,14 @@ void core_inverse_async(KeyRec& k, const uint32_t* in, const int64_t* sel, uint3
   core_inverse_async_raw(k, in, sel, out, count, tr, task, errp, st);
 }
 
-// Same, on a caller-provided tree buffer of 2 * padded ciphertexts.
+// Same, on a caller-provided tree buffer of 2 * padded ciphertexts.  With
+// inline_host the root is inverted by the calling thread after waiting for
+// the stream (the latency class of the server does this on its own
+// scheduler thread, so its batches never queue behind other streams' host
+// functions on the runtime's callback thread); otherwise by a host function
+// in stream order.
 void core_inverse_async_raw(KeyRec& k, const uint32_t* in, const int64_t* sel, uint32_t* out, size_t count,
-                            uint32_t* tr, InvTask& task, uint32_t* errp, cudaStream_t st) {
+                            uint32_t* tr, InvTask& task, uint32_t* errp, cudaStream_t st, bool inline_host) {
   if (count == 0) return;
   size_t padded = 1;
   while (padded < count) padded <<= 1;
@@ -563,7 +569,12 @@ void core_inverse_async_raw(KeyRec& k, const uint32_t* in, const int64_t* sel, u
   uint32_t* root = tr + off.back() * S;
   cuda_check(cudaMemcpyAsync(task.root, root, S * 4, cudaMemcpyDeviceToHost, st), "D2H root");
   cuda_check(cudaMemcpyAsync(task.root + S, errp, 4, cudaMemcpyDeviceToHost, st), "D2H err");
-  cuda_check(cudaLaunchHostFunc(st, inv_host_fn, &task), "host inversion");
+  if (inline_host) {
+    cuda_check(cudaStreamSynchronize(st), "stream sync");
+    inv_host_fn(&task);
+  } else {
+    cuda_check(cudaLaunchHostFunc(st, inv_host_fn, &task), "host inversion");
+  }
   cuda_check(cudaMemcpyAsync(root, task.z, S * 4, cudaMemcpyHostToDevice, st), "H2D inverse");
   for (size_t l = off.size() - 1; l-- > 0;) {
     const size_t up = padded >> (l + 1);
@@ -2742,6 +2753,9 @@ int hg_server_create(hg_ctx* ctx, const hg_server_config* cfg, hg_server** out) 
     if (s->express_len > 0) {
       s->sched = std::thread(scheduler, raw, 0);
       s->sched_express = std::thread(scheduler, raw, 1);
+      bool dec_slot = false;
+      for (auto& sl : s->slots) dec_slot |= sl->express_dec;
+      if (dec_slot) s->sched_express_slow = std::thread(scheduler, raw, 2);
     } else {
       s->sched = std::thread(scheduler, raw, -1);
     }
@@ -2760,6 +2774,7 @@ int hg_server_destroy(hg_server* s) {
     s->cv_work.notify_all();
     if (s->sched.joinable()) s->sched.join();
     if (s->sched_express.joinable()) s->sched_express.join();
+    if (s->sched_express_slow.joinable()) s->sched_express_slow.join();
     cudaSetDevice(s->ctx->device);
     for (auto& sl : s->slots) {
       cudaStreamSynchronize(sl->st);
@@ -2818,6 +2833,12 @@ int hg_server_submit(hg_server* s, const hg_request* req, uint64_t* ticket) {
     q->k = k;
     // the smallest slice must fit a slot (sums are never sliced)
     q->dev_bytes = slice_dev_bytes(*k, *req, req->op == kOpSum ? req->count : 1);
+    // a Mul with a negative scalar ends with a host inversion (a stream
+    // callback), which the express class keeps away from the other short ops
+    if (req->op == hg::kBatchMul && s->express_len > 0 && req->count <= s->express_len) {
+      const int64_t* kk = static_cast<const int64_t*>(req->in1);
+      for (size_t i = 0; i < req->count && !q->neg_scalar; ++i) q->neg_scalar = kk[i] < 0;
+    }
     if (q->dev_bytes > s->slots[0]->dev.cap) fail(HG_ERR_NOMEM, "request larger than a server slot");
     q->t_sub = std::chrono::steady_clock::now();
     {

@@ -51,6 +51,7 @@ struct Req {
   InvTask* task = nullptr;
   const void* p0 = nullptr;  // resolved resident vectors (set at admission, under the lock)
   const void* p1 = nullptr;
+  bool neg_scalar = false; // a short Mul with a negative scalar (express class 2)
   size_t next = 0;         // first element not yet handed to a micro-batch
   int outstanding = 0;     // slices on the GPU
   std::vector<std::unique_ptr<InvTask>> tasks;
@@ -124,7 +125,8 @@ struct hg_server {
   size_t regular_smem = 0;     // dynamic shared memory that keeps regular batches
                                // off the express slot's blocks on every SM
   std::thread sched;
-  std::thread sched_express;  // the express slots' scheduler (length rule)
+  std::thread sched_express;       // the express slot's scheduler (length rule)
+  std::thread sched_express_slow;  // the slow express slot's scheduler
 };
 
 namespace {
@@ -262,7 +264,9 @@ void run_slot(hg_server& s, Slot& sl) {
   }
   for (auto& iv : invs) {
     iv.task->status = 0;
-    core_inverse_async_raw(*iv.k, iv.data, iv.sel, iv.data, iv.count, iv.tree, *iv.task, err, st);
+    // express batches invert on their own scheduler thread (see
+    // core_inverse_async_raw), regular ones through a stream host function
+    core_inverse_async_raw(*iv.k, iv.data, iv.sel, iv.data, iv.count, iv.tree, *iv.task, err, st, sl.express);
   }
   for (auto& sj : sums) {
     KeyRec& k = *sj.q->k;
@@ -303,16 +307,19 @@ void finish_req(hg_server& s, Req* q) {
   s.cv_done.notify_all();
 }
 
-// Class of a pending request: 0 regular, 1 express, 2 express decrypt.
-// With express_len, short = at most express_len elements (short
-// decryptions get their own express slot when there is one); otherwise
-// short = estimated remaining work <= express_us.
+// Class of a pending request: 0 regular, 1 express, 2 slow express.
+// With express_len, short = at most express_len elements; short requests
+// whose batch would wait for a long dependent chain or a host step (CRT
+// decryptions, Mul with a negative scalar, which ends with a host
+// inversion) get the second express slot when there is one, so a batch of
+// the other short ops never waits for them.  Without express_len, short =
+// estimated remaining work <= express_us.
 int req_class(const hg_server& s, const Req* q) {
   if (s.express_len > 0) {
     if (q->r.count > s.express_len) return 0;
     bool dec_slot = false;
     for (auto& slp : s.slots) dec_slot |= slp->express_dec;
-    return (dec_slot && q->r.op == hg::kBatchDecrypt) ? 2 : 1;
+    return (dec_slot && (q->r.op == hg::kBatchDecrypt || q->neg_scalar)) ? 2 : 1;
   }
   if (s.express_us < 0.0) return 0;
   const double rem = elem_cost_us(*q->k, q->r.op) * (double)(q->r.count - q->next);
@@ -320,10 +327,15 @@ int req_class(const hg_server& s, const Req* q) {
 }
 
 // One scheduler thread serves the regular slots (which = 0) and, with the
-// length rule, another one the express slots (which = 1), so short requests
-// are staged and launched without waiting for the host work (staging,
-// planning) of a long batch; which = -1 serves every slot.
-bool serves(const Slot& sl, int which) { return which < 0 || sl.express == (which == 1); }
+// length rule, one thread each express slot (which = 1: the express slot,
+// 2: the slow express slot), so short requests are staged and launched
+// without waiting for the host work (staging, planning, inversions) of
+// another batch; which = -1 serves every slot.
+bool serves(const Slot& sl, int which) {
+  if (which < 0) return true;
+  if (which == 0) return !sl.express;
+  return sl.express && (sl.express_dec == (which == 2));
+}
 
 void scheduler(hg_server* sp, int which) {
   hg_server& s = *sp;
@@ -472,7 +484,7 @@ void scheduler(hg_server* sp, int which) {
         if (s.stop) return true;
         if (which < 0 || s.express_len == 0) return !s.pending.empty();
         for (const Req* q : s.pending)
-          if ((req_class(s, q) != 0) == (which == 1)) return true;
+          if (req_class(s, q) == which) return true;
         return false;
       };
       if (any_busy)

@@ -294,9 +294,11 @@ typedef struct {
                              elements run in the express slots, in the
                              latency layout of the batch kernel (a warp per
                              ciphertext), each batch as soon as a slot is
-                             free; with slots >= 3 short decryptions get an
-                             express slot of their own (slot 1), so the
-                             other short requests never wait for a CRT chain;
+                             free; with slots >= 3 short decryptions and
+                             short Muls with a negative scalar (which end
+                             with a host inversion) get an express slot of
+                             their own (slot 1), so the other short requests
+                             never wait for a CRT chain or a host step;
                              a scheduler thread of their own stages and
                              launches the express batches */
 } hg_server_config;
