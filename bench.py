@@ -256,7 +256,9 @@ def reference_arm(args):
         "metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
-        "data": "synthetic", "config": {"workload": WORKLOAD, "sample_elements_per_step": ns},
+        "data": "synthetic", "config": {"workload": WORKLOAD, "sample_elements_per_step": ns,
+                                        "sample_stands_for": "the 2^20-element step of the same workload: "
+                                                            "per-element work is identical, so ops/s compare"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -416,6 +418,9 @@ def ours_arm(args):
             eb.record(stream)
         torch.cuda.synchronize()
         per_op["mul_nonneg_k"] = n * args.steps / (ea.elapsed_time(eb) / 1e3)
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    mhz = (clocks or {}).get("sm_mhz") or (clocks or {}).get("sm_max_mhz")
+    issue_bound = 32 * sms * mhz * 1e6 / 1e12 if mhz else None
     macs_dec = decrypt_macs(KEY_BITS) * n
     dec_avg = op_s["decrypt"] / args.steps
     achieved = macs_dec / dec_avg / 1e12 if "decrypt" in ops else None
@@ -567,11 +572,21 @@ def ours_arm(args):
                        "l2": "inputs larger than L2 (512 MiB per ciphertext array); no flush",
                        "parallelism": f"replicas x{world}"},
             "per_op_ops_per_s": per_op,
+            "per_op_note": (f"encrypt uses a fixed-base table of window {args.window} "
+                            f"({encrypt_macs(KEY_BITS, args.window) // mm_macs(KEY_BITS // 16)} Montgomery "
+                            "multiplications per ciphertext, a time-memory trade of the 280 GB HBM) where the "
+                            "CPU restatement uses HEU's window 10 (105); the other ops run the same algorithms "
+                            "on both sides"),
             "roofline": {"bound": "imad", "kernel": "decrypt (CRT, k_decrypt)", "achieved": achieved,
                          "peak": peak, "unit": "TMAC/s", "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                          "peak_source": "measured live: hg_probe_mac_peak (best of mad.wide / carry-chain "
                                         "patterns); MEASURED_PEAKS.json has no integer figure",
                          "peak_chain_pattern": peak_chain, "peak_wide_pattern": peak_wide,
+                         # the issue bound of the wide multiply-add: 4 cycles per warp
+                         # instruction on each SM sub-partition's fmaheavy pipe = 32 MACs per
+                         # clock per SM, at the SM clock sampled during the timed region
+                         "issue_bound": issue_bound, "frac_of_issue_bound": (achieved / issue_bound)
+                         if (achieved and issue_bound) else None,
                          "per_op_tmacs": roof_ops},
             "parity_checked": parity_checked,
             "parity": ("strided sample of the timed Encrypt / Add / Mul outputs byte-equal (Montgomery form) to "
@@ -1319,7 +1334,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=1 << 20)
     ap.add_argument("--window", type=int, default=20)
-    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-parity", action="store_true", help="skip the post-timing byte comparison with paillier_z")

@@ -2,8 +2,8 @@
 and persists the chosen configuration per device and key size as JSON.
 
 The sweep (C++, in the engine) times encrypt and scalar mul for both
-(threads per ciphertext, limbs per thread) variants and mul windows 3..5,
-and CRT decrypt for both mod-p^2 variants and windows 4..6, then applies the
+(threads per ciphertext, limbs per thread) variants and mul windows 2..6,
+and CRT decrypt for both mod-p^2 variants and windows 4..7, then applies the
 fastest.  The configuration never changes results, only speed.
 """
 

@@ -2493,7 +2493,7 @@ int hg_autotune(hg_ctx* ctx, int key_id, size_t calib, hg_key_config* best, doub
       c.variant = v;
       apply_config(*k, c);
       const double te = timed([&] { core_encrypt(*k, w, hg::EncMode::kEncrypt, dm, nullptr, nullptr, dr, nullptr, dct, n); });
-      for (int wm = 3; wm <= 5; ++wm) {
+      for (int wm = 2; wm <= 6; ++wm) {
         c.mul_window = wm;
         apply_config(*k, c);
         const double tm = timed([&] {
@@ -2525,7 +2525,7 @@ int hg_autotune(hg_ctx* ctx, int key_id, size_t calib, hg_key_config* best, doub
       const size_t nd = std::min(n, std::max<size_t>(n / 2, 4 * wave));
       double best_d = 1e300;
       for (int dv = 0; dv < 2; ++dv)
-        for (int wd = 4; wd <= 6; ++wd) {
+        for (int wd = 4; wd <= 7; ++wd) {
           c.dec_variant = dv;
           c.dec_window = wd;
           apply_config(*k, c);

@@ -218,8 +218,8 @@ typedef struct {
 } hg_key_config;
 int hg_key_get_config(hg_ctx* ctx, int key_id, hg_key_config* out);
 int hg_key_set_config(hg_ctx* ctx, int key_id, const hg_key_config* cfg);
-/* Project autotuner: times encrypt and mul (both variants, mul windows 3..5)
- * and decrypt (both variants, windows 4..6) on `calib` random inputs
+/* Project autotuner: times encrypt and mul (both variants, mul windows 2..6)
+ * and decrypt (both variants, windows 4..7) on `calib` random inputs
  * (0 = 65536; decryption uses enough of them for several full waves),
  * applies the fastest configuration and returns it; rates[0..2] receive
  * encrypt, mul and decrypt ops/s at that configuration.  Calibrate with at
