@@ -1180,6 +1180,16 @@ def _latency_classes(lat, ops, lens, short_len):
     return out
 
 
+def _phase_p99(phases, ops, lens, short_len):
+    import numpy as np
+
+    m = (lens <= short_len) & ((ops == 0) | (ops == 2) | (ops == 4))
+    if not m.any():
+        return None
+    names = ("queued", "staged", "gpu_and_retire")
+    return {nm: float(np.percentile(phases[m, k], 99) * 1e3) for k, nm in enumerate(names)}
+
+
 def c5_measure(args, rates, nreq_for_rate):
     import numpy as np
     import torch
@@ -1244,6 +1254,8 @@ def c5_measure(args, rates, nreq_for_rate):
         ls.m_host, ls.r_host, ls.k_host, ls.sink = (m_host.data_ptr(), r_host.data_ptr(), k_host.data_ptr(),
                                                     sink.data_ptr())
         lat = np.zeros(nreq, dtype=np.float64)
+        phases = np.zeros((nreq, 3), dtype=np.float64)
+        ls.phases = phases.ctypes.data
         ops = np.zeros(nreq, dtype=np.int32)
         lens = np.zeros(nreq, dtype=np.uint64)
         wall = ctypes.c_double()
@@ -1260,6 +1272,8 @@ def c5_measure(args, rates, nreq_for_rate):
                         "p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
                         "mean_ms": float(lat.mean() * 1e3),
                         "classes": _latency_classes(lat, ops, lens, 1024),
+                        # short requests of encrypt / add / sum: p99 of each phase (ms)
+                        "short_eas_phases_p99_ms": _phase_p99(phases, ops, lens, 1024),
                         "throughput_req_per_s": nreq / wall.value,
                         "throughput_ops_per_s": float(lens.sum()) / wall.value,
                         "micro_batches": int(nb), "wall_s": wall.value})

@@ -152,7 +152,7 @@ class LoadSpec(ctypes.Structure):
                 ("rate", ctypes.c_double), ("nreq", ctypes.c_size_t), ("len_min", ctypes.c_size_t),
                 ("len_max", ctypes.c_size_t), ("op_weights", ctypes.c_double * 5), ("seed", ctypes.c_uint64),
                 ("m_host", ctypes.c_void_p), ("r_host", ctypes.c_void_p), ("k_host", ctypes.c_void_p),
-                ("sink", ctypes.c_void_p)]
+                ("sink", ctypes.c_void_p), ("phases", ctypes.c_void_p)]
 
 
 class KeyConfig(ctypes.Structure):

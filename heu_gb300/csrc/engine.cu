@@ -2855,16 +2855,25 @@ int hg_server_submit(hg_server* s, const hg_request* req, uint64_t* ticket) {
   });
 }
 
-int hg_server_wait(hg_server* s, uint64_t ticket, double* latency_s) {
+namespace {
+
+// hg_server_wait, with the request's phases (3 values, may be null).
+int server_wait(hg_server* s, uint64_t ticket, double* latency_s, double* phases) {
   int status = HG_OK;
-  const int rc = guarded(__func__, [&] {
+  const int rc = guarded("hg_server_wait", [&] {
     if (!s) fail(HG_ERR_INVALID, "null server");
     std::unique_lock<std::mutex> lk(s->mu);
     auto it = s->reqs.find(ticket);
     if (it == s->reqs.end()) fail(HG_ERR_INVALID, "unknown ticket");
     Req* q = it->second.get();
     s->cv_done.wait(lk, [&] { return q->done; });
-    if (latency_s) latency_s[0] = std::chrono::duration<double>(q->t_done - q->t_sub).count();
+    auto sec = [](std::chrono::steady_clock::duration d) { return std::chrono::duration<double>(d).count(); };
+    if (latency_s) latency_s[0] = sec(q->t_done - q->t_sub);
+    if (phases) {
+      phases[0] = sec(q->t_admit - q->t_sub);
+      phases[1] = sec(q->t_launch - q->t_admit);
+      phases[2] = sec(q->t_done - q->t_launch);
+    }
     status = q->status;
     s->reqs.erase(it);
     return HG_OK;
@@ -2872,6 +2881,12 @@ int hg_server_wait(hg_server* s, uint64_t ticket, double* latency_s) {
   if (rc != HG_OK) return rc;
   if (status != HG_OK) g_last_error = "request failed";
   return status;
+}
+
+}  // namespace
+
+int hg_server_wait(hg_server* s, uint64_t ticket, double* latency_s) {
+  return server_wait(s, ticket, latency_s, nullptr);
 }
 
 int hg_server_stats(hg_server* s, uint64_t* completed, uint64_t* batches, size_t* inflight_bytes, size_t* pending) {
@@ -2930,7 +2945,10 @@ int hg_probe_serve_load(hg_server* s, const hg_load_spec* spec, double* latencie
       if (lens) lens[i] = len;
     }
     for (size_t i = 0; i < spec->nreq; ++i) {
-      const int rc = hg_server_wait(s, tickets[i], &latencies[i]);
+      double ph[3];
+      const int rc = server_wait(s, tickets[i], &latencies[i], spec->phases ? ph : nullptr);
+      if (spec->phases)
+        for (int k = 0; k < 3; ++k) spec->phases[3 * i + k] = ph[k];
       if (rc != HG_OK) fail(rc, "served request failed");
     }
     if (wall_s) *wall_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();

@@ -46,6 +46,7 @@ struct Req {
   uint64_t id = 0;
   size_t dev_bytes = 0;
   std::chrono::steady_clock::time_point t_sub, t_done;
+  std::chrono::steady_clock::time_point t_admit, t_launch;  // first slice: admitted, its batch launched
   int status = HG_OK;
   bool done = false;
   InvTask* task = nullptr;
@@ -440,6 +441,7 @@ void scheduler(hg_server* sp, int which) {
           tp = task.get();
           q->tasks.push_back(std::move(task));
         }
+        if (q->next == 0) q->t_admit = std::chrono::steady_clock::now();
         sl.slices.push_back({q, q->next, len, need, tp});
         q->next += len;
         q->outstanding++;
@@ -459,6 +461,9 @@ void scheduler(hg_server* sp, int which) {
       lk.unlock();
       try {
         run_slot(s, sl);
+        const auto now = std::chrono::steady_clock::now();
+        for (Slice& sc : sl.slices)
+          if (sc.start == 0) sc.q->t_launch = now;
       } catch (const HgError& e) {
         cudaStreamSynchronize(sl.st);
         lk.lock();

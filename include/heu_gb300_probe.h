@@ -54,6 +54,9 @@ typedef struct {
   const void* r_host;
   const void* k_host;
   void* sink;
+  double* phases;  /* optional, 3 x nreq: per request the seconds from submission to
+                      its first micro-batch, staging and launch of that batch, and from
+                      the launch to completion (the last slice's batch retired) */
 } hg_load_spec;
 int hg_probe_serve_load(hg_server* s, const hg_load_spec* spec, double* latencies, int* ops, uint64_t* lens,
                         double* wall_s);

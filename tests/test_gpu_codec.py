@@ -109,10 +109,22 @@ def test_batch_encoder_on_device(gpu_key, padding):
         be = hnp.BatchEncoder(scale, padding)
         mags = be.pack(a, b, key.pt_limbs)
         assert np.array_equal(ct, key.encrypt_bn(hg.limbs_to_ints(mags), r))
-    # Add of packed ciphertexts adds the slots; decode per slot
+    # Add of packed ciphertexts adds the slots; decode per slot: the low 64
+    # bits of each slot as int64, / scale with C++ division (batch_encoder.h:
+    # 85-103), so a doubled slot wraps like the int64 it is read as
+    def slot_sum(vals):
+        out = []
+        for v in vals:
+            w = (2 * int(v) * scale) & mask
+            w = w - 2 ** 64 if w >= 2 ** 63 else w
+            q = abs(w) // scale
+            out.append(-q if w < 0 else q)
+        return np.array(out, dtype=np.int64)
+
     s0, s1, neg = key.decrypt_decoded(capi.HG_CODEC_BATCH_I64, scale, key.add(ct, ct), padding_bits=padding)
     assert neg.sum() == 0
-    assert np.array_equal(s0, 2 * a) and np.array_equal(s1, 2 * b)
+    assert np.array_equal(s0, slot_sum(a)) and np.array_equal(s1, slot_sum(b))
+    assert np.array_equal(s0[4:], 2 * a[4:]) and np.array_equal(s1, 2 * b)
     f0, f1, _ = key.decrypt_decoded(capi.HG_CODEC_BATCH_F64, scale, ct, padding_bits=padding)
     assert np.array_equal(f0, (a * scale).astype(np.float64) / scale)
     # double inputs: int64(trunc(x * scale))
