@@ -680,7 +680,7 @@ int current_sm_count() {
 void core_sum(KeyRec& k, Work& w, const uint32_t* a, size_t count, uint32_t* out) {
   if (count == 0) fail(HG_ERR_INVALID, "you cannot sum an empty tensor");
   const size_t S = (size_t)k.S;
-  const size_t target = (size_t)std::max(1, current_sm_count() * 4 * hg::instances_per_block(k.S, k.kc.variant));
+  const size_t target = (size_t)std::max(1, current_sm_count() * 4 * hg::instances_per_block(k.S, 0));
   const uint32_t* cur = a;
   size_t n = count;
   int which = 0;
@@ -688,11 +688,13 @@ void core_sum(KeyRec& k, Work& w, const uint32_t* a, size_t count, uint32_t* out
     cuda_check(cudaMemcpyAsync(out, a, S * 4, cudaMemcpyDeviceToDevice, w.stream), "copy");
     return;
   }
+  // tree levels: groups multiply chunks, blocks combine their groups by warp
+  // shuffles (one output per block); about three levels for 2^20 inputs
   while (n > 1) {
-    int chunk = (int)std::min<size_t>(64, std::max<size_t>(2, (n + target - 1) / target));
-    const size_t outn = (n + chunk - 1) / chunk;
+    const int chunk = (int)std::min<size_t>(64, std::max<size_t>(2, (n + target - 1) / target));
+    const size_t outn = hg::reduce_tree_outputs(k.S, n, chunk);
     uint32_t* dst = (outn == 1) ? out : w.red[which].ensure<uint32_t>(outn * S * 4);
-    cuda_check(hg::launch_reduce(k.S, k.kc, cur, n, chunk, dst, w.errp(), w.stream), "reduce launch");
+    cuda_check(hg::launch_reduce_tree(k.S, k.kc, cur, n, chunk, dst, w.errp(), w.stream), "reduce launch");
     cur = dst;
     n = outn;
     which ^= 1;

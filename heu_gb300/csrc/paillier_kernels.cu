@@ -165,6 +165,61 @@ __global__ void __launch_bounds__(kBlock) k_reduce(KeyConst kc, const uint32_t* 
   if (active) store_slice<L>(out + i * S + g.t * L, acc);
 }
 
+// Sum as a tree of modular products (numpy/evaluator.cc:355-373 reduces with
+// AddInplace = MulMod): each group of TPI lanes multiplies its chunk of
+// `chunk` inputs in sequence (every input range-checked), then the groups of
+// a warp combine pairwise through shuffles (log2(32/TPI) levels, one
+// Montgomery multiplication each), and warp 0 multiplies in the other warps'
+// products from shared memory: one ciphertext per block, out[blockIdx.x].
+// Missing inputs count as the identity R.
+template <int TPI, int L>
+__global__ void __launch_bounds__(kBlock) k_reduce_tree(KeyConst kc, const uint32_t* __restrict__ in, size_t count,
+                                                        int chunk, uint32_t* __restrict__ out, uint32_t* err) {
+  constexpr int S = TPI * L;
+  constexpr int IPW = 32 / TPI;
+  constexpr int kWarps = kBlock / 32;
+  __shared__ __align__(16) uint32_t wsum[kWarps][S];
+  const Group<TPI> g;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const size_t inst = ((size_t)blockIdx.x * kBlock + threadIdx.x) / TPI;
+  uint32_t N[L], acc[L];
+  load_slice<L>(N, kc.N + g.t * L);
+  load_slice<L>(acc, kc.R1 + g.t * L);
+  const size_t first = inst * (size_t)chunk;
+#pragma unroll 1
+  for (int j = 0; j < chunk; ++j) {
+    const size_t idx = first + j;
+    const bool valid = idx < count;
+    if (!__any_sync(kFull, valid)) break;
+    uint32_t B[L];
+    load_slice<L>(B, (valid ? in + idx * S : kc.R1) + g.t * L);
+    check_ct<TPI, L>(B, N, valid, g, err);
+    mont_mul<TPI, L>(acc, acc, B, N, kc.np, g);
+  }
+  // groups of the warp: group k takes group k + d's product (k % 2d == 0)
+#pragma unroll
+  for (int d = 1; d < IPW; d <<= 1) {
+    uint32_t B[L];
+#pragma unroll
+    for (int j = 0; j < L; ++j) B[j] = __shfl_down_sync(kFull, acc[j], d * TPI);
+    const bool take = ((lane / TPI) % (2 * d) == 0) && (lane / TPI + d < IPW);
+    if (!take) load_slice<L>(B, kc.R1 + g.t * L);
+    mont_mul<TPI, L>(acc, acc, B, N, kc.np, g);
+  }
+  if (lane < TPI) store_slice<L>(&wsum[warp][g.t * L], acc);
+  __syncthreads();
+  if (warp == 0) {
+    // warp 0 multiplies the other warps' products into its own
+#pragma unroll
+    for (int w = 1; w < kWarps; ++w) {
+      uint32_t B[L];
+      load_slice<L>(B, &wsum[w][g.t * L]);
+      mont_mul<TPI, L>(acc, acc, B, N, kc.np, g);
+    }
+    if (lane < TPI) store_slice<L>(out + (size_t)blockIdx.x * S + g.t * L, acc);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Product tree for batch inversion (Montgomery's simultaneous-inversion
 // trick arranged as a tree): leaves, up-sweep, root fix, down-sweep, apply.
@@ -472,6 +527,23 @@ cudaError_t launch_reduce(int S, const KeyConst& kc, const uint32_t* in, size_t 
                  k_reduce<TPI, L><<<blocks_for(out_count, TPI), kBlock, 0, st>>>(kc, in, count, chunk, out,
                                                                                  out_count, err));
   return counted();
+}
+
+cudaError_t launch_reduce_tree(int S, const KeyConst& kc, const uint32_t* in, size_t count, int chunk,
+                               uint32_t* out, uint32_t* err, cudaStream_t st) {
+  if (count == 0) return cudaSuccess;
+  HG_DISPATCH_S0(S, {
+    const size_t per_block = (size_t)(kBlock / TPI) * (size_t)chunk;
+    const unsigned blocks = (unsigned)((count + per_block - 1) / per_block);
+    k_reduce_tree<TPI, L><<<blocks, kBlock, 0, st>>>(kc, in, count, chunk, out, err);
+  });
+  return counted();
+}
+
+size_t reduce_tree_outputs(int S, size_t count, int chunk) {
+  const int tpi = S == 64 ? 4 : S == 128 ? 8 : 16;
+  const size_t per_block = (size_t)(kBlock / tpi) * (size_t)chunk;
+  return (count + per_block - 1) / per_block;
 }
 
 cudaError_t launch_tree_leaves(int S, const KeyConst& kc, const uint32_t* in, const int64_t* sel, size_t count,

@@ -136,6 +136,12 @@ cudaError_t launch_mul_const(int S, const KeyConst& kc, const uint32_t* in, cons
                              size_t count, uint32_t* err, cudaStream_t st);
 cudaError_t launch_convert(int S, const KeyConst& kc, const uint32_t* in, uint32_t* out, size_t count,
                            int to_mont, uint32_t* err, cudaStream_t st);
+// Sum as a tree: groups multiply chunks of `chunk` inputs, then combine by
+// warp shuffles and shared memory into one ciphertext per block of the
+// default layout; reduce_tree_outputs(S, count, chunk) blocks = outputs.
+cudaError_t launch_reduce_tree(int S, const KeyConst& kc, const uint32_t* in, size_t count, int chunk,
+                               uint32_t* out, uint32_t* err, cudaStream_t st);
+size_t reduce_tree_outputs(int S, size_t count, int chunk);
 cudaError_t launch_reduce(int S, const KeyConst& kc, const uint32_t* in, size_t count, int chunk,
                           uint32_t* out, uint32_t* err, cudaStream_t st);
 // product tree for batch inversion

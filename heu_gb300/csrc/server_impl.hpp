@@ -279,9 +279,9 @@ void run_slot(hg_server& s, Slot& sl) {
     }
     while (n > 1) {
       const int chunk = (int)std::min<size_t>(64, std::max<size_t>(2, (n + 4095) / 4096));
-      const size_t on = (n + chunk - 1) / chunk;
+      const size_t on = hg::reduce_tree_outputs(k.S, n, chunk);
       uint32_t* dst = on == 1 ? sj.out : sj.bufs[which];
-      cuda_check(hg::launch_reduce(k.S, k.kc, cur, n, chunk, dst, err, st), "reduce");
+      cuda_check(hg::launch_reduce_tree(k.S, k.kc, cur, n, chunk, dst, err, st), "reduce");
       cur = dst;
       n = on;
       which ^= 1;
