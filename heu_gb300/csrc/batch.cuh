@@ -45,6 +45,9 @@ __host__ __device__ constexpr int tp_for(int SP, int V) {
 constexpr int kBatchLatencyVariant = 2;
 
 int batch_resident_blocks(int variant);
+// Every variant of the batch kernel prefers the largest shared-memory carveout
+// (see server_prefer_shared_carveout).
+void batch_prefer_shared_carveout();
 int batch_warps_per_block();
 cudaError_t launch_batch(int variant, const BatchJob* jobs, const BatchTile* tiles, uint32_t ntiles,
                          uint32_t* counter, uint32_t* scratch, size_t warp_words, uint32_t* err, int grid,

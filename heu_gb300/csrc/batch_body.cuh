@@ -138,6 +138,9 @@ void count_launches(uint64_t n);
 
 // The three entry points of one variant set, defined by batch_v<V>.cu.
 #define HG_BATCH_VARIANT_ENTRY_POINTS(V)                                                                      \
+  void batch_carveout_v##V(int pct) {                                                                       \
+    cudaFuncSetAttribute(k_batch<V>, cudaFuncAttributePreferredSharedMemoryCarveout, pct);                  \
+  }                                                                                                         \
   int batch_resident_blocks_v##V() { return batch_occupancy_blocks(k_batch<V>); }                          \
   size_t batch_smem_cap_v##V(int blocks_per_sm) { return batch_smem_cap_pad(k_batch<V>, blocks_per_sm); } \
   cudaError_t launch_batch_v##V(const BatchJob* jobs, const BatchTile* tiles, uint32_t ntiles,              \

@@ -8,6 +8,7 @@
 namespace hg {
 
 #define HG_BATCH_DECLARE(V)                                                                                  \
+  void batch_carveout_v##V(int pct);                                                                         \
   int batch_resident_blocks_v##V();                                                                          \
   size_t batch_smem_cap_v##V(int blocks_per_sm);                                                             \
   cudaError_t launch_batch_v##V(const BatchJob* jobs, const BatchTile* tiles, uint32_t ntiles,               \
@@ -30,6 +31,12 @@ int batch_resident_blocks(int variant) {
 }
 
 int batch_warps_per_block() { return kWarps; }
+
+void batch_prefer_shared_carveout() {
+  batch_carveout_v0(100);
+  batch_carveout_v1(100);
+  batch_carveout_v2(100);
+}
 
 cudaError_t launch_batch(int variant, const BatchJob* jobs, const BatchTile* tiles, uint32_t ntiles,
                          uint32_t* counter, uint32_t* scratch, size_t warp_words, uint32_t* err, int grid,

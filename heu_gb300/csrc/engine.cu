@@ -2694,6 +2694,10 @@ int hg_server_create(hg_ctx* ctx, const hg_server_config* cfg, hg_server** out) 
     if (cfg && cfg->slice_us > 0) s->slice_us = cfg->slice_us;
     if (cfg && (cfg->policy < 0 || cfg->policy > 1)) fail(HG_ERR_INVALID, "policy must be 0 or 1");
     s->policy = cfg ? cfg->policy : 0;
+    // every kernel the server launches asks for the same L1 / shared split,
+    // so no SM has to drain to switch between them
+    hg::batch_prefer_shared_carveout();
+    hg::server_prefer_shared_carveout();
     const int resident = hg::batch_resident_blocks(c.variant);
     const int bps = hg::batch_blocks_per_sm(c.variant);
     const int sms = std::max(1, resident / std::max(1, bps));

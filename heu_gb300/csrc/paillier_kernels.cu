@@ -540,6 +540,25 @@ cudaError_t launch_reduce_tree(int S, const KeyConst& kc, const uint32_t* in, si
   return counted();
 }
 
+// The serving loop runs these kernels next to persistent batch kernels that
+// take the largest shared-memory carveout; an SM changes its L1 / shared
+// split only when it is idle, so a kernel preferring another split would wait
+// for the long batches to drain.  All of them prefer the same split.
+void server_prefer_shared_carveout() {
+  auto set = [](const void* f) { cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, 100); };
+#define HG_CARVE(TPI, L)                                                  \
+  set((const void*)k_reduce_tree<TPI, L>);                                \
+  set((const void*)k_reduce<TPI, L>);                                     \
+  set((const void*)k_tree_leaves<TPI, L>);                                \
+  set((const void*)k_tree_up<TPI, L>);                                    \
+  set((const void*)k_tree_down<TPI, L>);                                  \
+  set((const void*)k_tree_apply<TPI, L>);
+  HG_CARVE(4, 16)
+  HG_CARVE(8, 16)
+  HG_CARVE(16, 12)
+#undef HG_CARVE
+}
+
 size_t reduce_tree_outputs(int S, size_t count, int chunk) {
   const int tpi = S == 64 ? 4 : S == 128 ? 8 : 16;
   const size_t per_block = (size_t)(kBlock / tpi) * (size_t)chunk;

@@ -142,6 +142,9 @@ cudaError_t launch_convert(int S, const KeyConst& kc, const uint32_t* in, uint32
 cudaError_t launch_reduce_tree(int S, const KeyConst& kc, const uint32_t* in, size_t count, int chunk,
                                uint32_t* out, uint32_t* err, cudaStream_t st);
 size_t reduce_tree_outputs(int S, size_t count, int chunk);
+// The reduction and inversion-tree kernels prefer the largest shared-memory
+// carveout, as the batch kernels do (serving loop).
+void server_prefer_shared_carveout();
 cudaError_t launch_reduce(int S, const KeyConst& kc, const uint32_t* in, size_t count, int chunk,
                           uint32_t* out, uint32_t* err, cudaStream_t st);
 // product tree for batch inversion
