@@ -19,6 +19,10 @@ import argparse
 import ctypes
 import json
 import os
+
+# before any CUDA context exists: every stream its own hardware work queue
+# (the request server's slots must not queue behind one another's kernels)
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 import statistics
 import subprocess
 import sys

@@ -115,6 +115,7 @@ SIGNATURES = {
     "hg_server_wait": [_P, _U64, ctypes.POINTER(ctypes.c_double)],
     "hg_server_stats": [_P, ctypes.POINTER(_U64), ctypes.POINTER(_U64), ctypes.POINTER(_SZ), ctypes.POINTER(_SZ)],
     "hg_probe_serve_load": [_P, _P, _P, _P, _P, ctypes.POINTER(ctypes.c_double)],
+    "hg_probe_server_trace": [_P, _I, _P, _SZ, ctypes.POINTER(_SZ)],
     "hg_probe_mac_peak": [_I, _I, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)],
     "hg_probe_launch_count": [ctypes.POINTER(_U64)],
     "hg_probe_set_alloc_limit": [_SZ, ctypes.POINTER(_SZ)],

@@ -5,6 +5,7 @@
 #include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <chrono>
 #include <random>
@@ -12,6 +13,7 @@
 #include <deque>
 #include <thread>
 #include <unordered_map>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -680,7 +682,7 @@ int current_sm_count() {
 void core_sum(KeyRec& k, Work& w, const uint32_t* a, size_t count, uint32_t* out) {
   if (count == 0) fail(HG_ERR_INVALID, "you cannot sum an empty tensor");
   const size_t S = (size_t)k.S;
-  const size_t target = (size_t)std::max(1, current_sm_count() * 4 * hg::instances_per_block(k.S, 0));
+  const int sms = current_sm_count();
   const uint32_t* cur = a;
   size_t n = count;
   int which = 0;
@@ -689,9 +691,9 @@ void core_sum(KeyRec& k, Work& w, const uint32_t* a, size_t count, uint32_t* out
     return;
   }
   // tree levels: groups multiply chunks, blocks combine their groups by warp
-  // shuffles (one output per block); about three levels for 2^20 inputs
+  // shuffles (one output per block); three levels for 2^20 inputs
   while (n > 1) {
-    const int chunk = (int)std::min<size_t>(64, std::max<size_t>(2, (n + target - 1) / target));
+    const int chunk = hg::reduce_tree_chunk(k.S, n, sms);
     const size_t outn = hg::reduce_tree_outputs(k.S, n, chunk);
     uint32_t* dst = (outn == 1) ? out : w.red[which].ensure<uint32_t>(outn * S * 4);
     cuda_check(hg::launch_reduce_tree(k.S, k.kc, cur, n, chunk, dst, w.errp(), w.stream), "reduce launch");
@@ -1198,6 +1200,13 @@ int hg_ctx_create(int device, hg_ctx** out) {
     if (!out) fail(HG_ERR_INVALID, "null out pointer");
     auto ctx = std::make_unique<hg_ctx>();
     ctx->device = device;
+    // Streams share the device's hardware work queues round-robin (8 by
+    // default); a stream whose next command waits on its own kernel then
+    // holds up every stream behind it in the same queue.  The server's slots
+    // must not wait on one another that way, so ask for the most queues
+    // unless the user has chosen a number; this takes effect when the
+    // process's CUDA context is created by the call below.
+    setenv("CUDA_DEVICE_MAX_CONNECTIONS", "32", 0);
     cuda_check(cudaSetDevice(device), "cudaSetDevice");
     hg::forget_noalloc_scratch(device);
     cuda_check(cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device), "attr");
@@ -2701,6 +2710,7 @@ int hg_server_create(hg_ctx* ctx, const hg_server_config* cfg, hg_server** out) 
     const int resident = hg::batch_resident_blocks(c.variant);
     const int bps = hg::batch_blocks_per_sm(c.variant);
     const int sms = std::max(1, resident / std::max(1, bps));
+    s->sms = current_sm_count();
     s->express_us = (cfg && cfg->express_us != 0.0) ? cfg->express_us : -1.0;
     s->express_len = cfg ? cfg->express_len : 0;
     if (s->express_len > 0) s->express_us = 0.0;  // the length rule replaces the cost rule
@@ -2746,6 +2756,7 @@ int hg_server_create(hg_ctx* ctx, const hg_server_config* cfg, hg_server** out) 
       cuda_check(cudaStreamCreateWithPriority(&sl->st, cudaStreamNonBlocking, sl->express ? hi_prio : lo_prio),
                  "stream");
       cuda_check(cudaEventCreateWithFlags(&sl->ev, cudaEventDisableTiming), "event");
+      for (auto& e : sl->tev) cuda_check(cudaEventCreate(&e), "trace event");
       sl->dev.base = sl->dev_mem.ensure<uint8_t>(arena);
       sl->dev.cap = arena;
       sl->pin.base = sl->pin_mem.ensure<uint8_t>((size_t)16 << 20);
@@ -2786,7 +2797,10 @@ int hg_server_destroy(hg_server* s) {
       cudaStreamSynchronize(sl->st);
       cudaStreamDestroy(sl->st);
       cudaEventDestroy(sl->ev);
+      for (auto& e : sl->tev)
+        if (e) cudaEventDestroy(e);
     }
+    if (s->trace_ref) cudaEventDestroy(s->trace_ref);
     delete s;
     return HG_OK;
   });
@@ -2839,12 +2853,6 @@ int hg_server_submit(hg_server* s, const hg_request* req, uint64_t* ticket) {
     q->k = k;
     // the smallest slice must fit a slot (sums are never sliced)
     q->dev_bytes = slice_dev_bytes(*k, *req, req->op == kOpSum ? req->count : 1);
-    // a Mul with a negative scalar ends with a host inversion (a stream
-    // callback), which the express class keeps away from the other short ops
-    if (req->op == hg::kBatchMul && s->express_len > 0 && req->count <= s->express_len) {
-      const int64_t* kk = static_cast<const int64_t*>(req->in1);
-      for (size_t i = 0; i < req->count && !q->neg_scalar; ++i) q->neg_scalar = kk[i] < 0;
-    }
     if (q->dev_bytes > s->slots[0]->dev.cap) fail(HG_ERR_NOMEM, "request larger than a server slot");
     q->t_sub = std::chrono::steady_clock::now();
     {
@@ -2958,6 +2966,35 @@ int hg_probe_serve_load(hg_server* s, const hg_load_spec* spec, double* latencie
       if (rc != HG_OK) fail(rc, "served request failed");
     }
     if (wall_s) *wall_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return HG_OK;
+  });
+}
+
+int hg_probe_server_trace(hg_server* s, int enable, double* records, size_t cap, size_t* n) {
+  return guarded(__func__, [&] {
+    if (!s) fail(HG_ERR_INVALID, "null server");
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (enable) {
+      set_device(s->ctx);
+      if (!s->trace_ref) cuda_check(cudaEventCreate(&s->trace_ref), "trace event");
+      s->traces.clear();
+      // the reference event goes on an idle slot's stream, so the GPU takes
+      // its time stamp when the host does
+      cudaStream_t st = nullptr;
+      for (auto& sl : s->slots)
+        if (!sl->busy) st = sl->st;
+      if (!st) fail(HG_ERR_INVALID, "trace enabled while every slot is busy");
+      s->trace_t0 = std::chrono::steady_clock::now();
+      cuda_check(cudaEventRecord(s->trace_ref, st), "trace event");
+      s->trace = true;
+      if (n) *n = 0;
+      return HG_OK;
+    }
+    s->trace = false;
+    if (n) *n = s->traces.size();
+    if (records)
+      for (size_t i = 0; i < std::min(cap, s->traces.size()); ++i)
+        std::memcpy(records + i * kTraceFields, s->traces[i].data(), sizeof(double) * kTraceFields);
     return HG_OK;
   });
 }

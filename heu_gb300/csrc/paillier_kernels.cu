@@ -194,7 +194,13 @@ __global__ void __launch_bounds__(kBlock) k_reduce_tree(KeyConst kc, const uint3
     uint32_t B[L];
     load_slice<L>(B, (valid ? in + idx * S : kc.R1) + g.t * L);
     check_ct<TPI, L>(B, N, valid, g, err);
-    mont_mul<TPI, L>(acc, acc, B, N, kc.np, g);
+    if (j == 0) {
+      // the first input starts the product (acc is R, the identity)
+#pragma unroll
+      for (int t = 0; t < L; ++t) acc[t] = B[t];
+    } else {
+      mont_mul<TPI, L>(acc, acc, B, N, kc.np, g);
+    }
   }
   // groups of the warp: group k takes group k + d's product (k % 2d == 0)
 #pragma unroll
@@ -206,18 +212,21 @@ __global__ void __launch_bounds__(kBlock) k_reduce_tree(KeyConst kc, const uint3
     if (!take) load_slice<L>(B, kc.R1 + g.t * L);
     mont_mul<TPI, L>(acc, acc, B, N, kc.np, g);
   }
+  // warps of the block, as a tree through shared memory: warp w takes warp
+  // w + d's product (w % 2d == 0); warp 0 ends with the block's product
   if (lane < TPI) store_slice<L>(&wsum[warp][g.t * L], acc);
   __syncthreads();
-  if (warp == 0) {
-    // warp 0 multiplies the other warps' products into its own
 #pragma unroll
-    for (int w = 1; w < kWarps; ++w) {
+  for (int d = 1; d < kWarps; d <<= 1) {
+    if (warp % (2 * d) == 0 && warp + d < kWarps) {
       uint32_t B[L];
-      load_slice<L>(B, &wsum[w][g.t * L]);
+      load_slice<L>(B, &wsum[warp + d][g.t * L]);
       mont_mul<TPI, L>(acc, acc, B, N, kc.np, g);
+      if (lane < TPI) store_slice<L>(&wsum[warp][g.t * L], acc);
     }
-    if (lane < TPI) store_slice<L>(out + (size_t)blockIdx.x * S + g.t * L, acc);
+    __syncthreads();
   }
+  if (warp == 0 && lane < TPI) store_slice<L>(out + (size_t)blockIdx.x * S + g.t * L, acc);
 }
 
 // ---------------------------------------------------------------------------
@@ -563,6 +572,22 @@ size_t reduce_tree_outputs(int S, size_t count, int chunk) {
   const int tpi = S == 64 ? 4 : S == 128 ? 8 : 16;
   const size_t per_block = (size_t)(kBlock / tpi) * (size_t)chunk;
   return (count + per_block - 1) / per_block;
+}
+
+int reduce_tree_chunk(int S, size_t count, int sms) {
+  const int tpi = S == 64 ? 4 : S == 128 ? 8 : 16;
+  const size_t gpb = (size_t)(kBlock / tpi);
+  // blocks of this instance resident on one SM (register-limited)
+  int per_sm = 0;
+  if (S == 64) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_reduce_tree<4, 16>, kBlock, 0);
+  if (S == 128) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_reduce_tree<8, 16>, kBlock, 0);
+  if (S == 192) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_reduce_tree<16, 12>, kBlock, 0);
+  const size_t resident = (size_t)std::max(1, sms) * (size_t)std::max(1, per_sm) * gpb;
+  // a few inputs per group: one block finishes the sum
+  if (count <= 4 * gpb) return (int)((count + gpb - 1) / gpb);
+  // more inputs than resident groups: one full wave, every group the same
+  // number of inputs; fewer: one input per group (latency-bound levels)
+  return (int)std::max<size_t>(1, (count + resident - 1) / resident);
 }
 
 cudaError_t launch_tree_leaves(int S, const KeyConst& kc, const uint32_t* in, const int64_t* sel, size_t count,

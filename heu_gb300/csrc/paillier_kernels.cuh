@@ -142,6 +142,10 @@ cudaError_t launch_convert(int S, const KeyConst& kc, const uint32_t* in, uint32
 cudaError_t launch_reduce_tree(int S, const KeyConst& kc, const uint32_t* in, size_t count, int chunk,
                                uint32_t* out, uint32_t* err, cudaStream_t st);
 size_t reduce_tree_outputs(int S, size_t count, int chunk);
+// Chunk of one tree level over `count` inputs on `sms` multiprocessors: one
+// full wave of groups while inputs outnumber the resident groups, one input
+// per group below that, one block for the last few inputs.
+int reduce_tree_chunk(int S, size_t count, int sms);
 // The reduction and inversion-tree kernels prefer the largest shared-memory
 // carveout, as the batch kernels do (serving loop).
 void server_prefer_shared_carveout();

@@ -52,7 +52,6 @@ struct Req {
   InvTask* task = nullptr;
   const void* p0 = nullptr;  // resolved resident vectors (set at admission, under the lock)
   const void* p1 = nullptr;
-  bool neg_scalar = false; // a short Mul with a negative scalar (express class 2)
   size_t next = 0;         // first element not yet handed to a micro-batch
   int outstanding = 0;     // slices on the GPU
   std::vector<std::unique_ptr<InvTask>> tasks;
@@ -78,7 +77,15 @@ struct Slot {
   bool busy = false;
   bool express = false;      // runs short requests on a reserved share of every SM
   bool express_dec = false;  // the express slot of short decryptions
+  // per-batch trace (probe): timing events around the staged copies, the
+  // kernels and the copies back, and the host times of the batch
+  cudaEvent_t tev[4] = {nullptr, nullptr, nullptr, nullptr};
+  bool traced = false;
+  double tr[6] = {0, 0, 0, 0, 0, 0};  // class, slices, elems, op mask, formed, launched
 };
+
+// Fields of one trace record (hg_probe_server_trace).
+constexpr int kTraceFields = 12;
 
 size_t slice_dev_bytes(const KeyRec& k, const hg_request& r, size_t n) {
   const size_t cb = (size_t)k.S * 4, pad = 256;
@@ -123,11 +130,16 @@ struct hg_server {
   size_t express_len = 0;      // > 0: short = at most this many elements, run in the latency layout
   int express_grid = 0;        // batch-kernel blocks of the express slot
   int regular_grid = 0;        // batch-kernel blocks of every other slot
+  int sms = 1;                 // multiprocessors of the server's device
   size_t regular_smem = 0;     // dynamic shared memory that keeps regular batches
                                // off the express slot's blocks on every SM
   std::thread sched;
   std::thread sched_express;       // the express slot's scheduler (length rule)
   std::thread sched_express_slow;  // the slow express slot's scheduler
+  bool trace = false;              // record one trace record per retired batch
+  std::chrono::steady_clock::time_point trace_t0;
+  cudaEvent_t trace_ref = nullptr;  // GPU time zero of the trace
+  std::vector<std::array<double, kTraceFields>> traces;
 };
 
 namespace {
@@ -174,6 +186,7 @@ void run_slot(hg_server& s, Slot& sl) {
   };
   std::vector<InvJob> invs;
   uint32_t* err = sl.err.as<uint32_t>();
+  if (sl.traced) cuda_check(cudaEventRecord(sl.tev[0], st), "trace event");
   cuda_check(cudaMemsetAsync(err, 0, 4, st), "memset err");
   for (Slice& sc : sl.slices) {
     Req* q = sc.q;
@@ -248,6 +261,7 @@ void run_slot(hg_server& s, Slot& sl) {
     cuda_check(cudaMemcpyAsync(dj, hj, jb, cudaMemcpyHostToDevice, st), "H2D jobs");
     cuda_check(cudaMemcpyAsync(dt, ht, tb, cudaMemcpyHostToDevice, st), "H2D tiles");
     cuda_check(cudaMemsetAsync(sl.counter.p, 0, 4, st), "memset counter");
+    if (sl.traced) cuda_check(cudaEventRecord(sl.tev[1], st), "trace event");
     // the express slots split the reserved blocks, so neither waits for the
     // other's blocks to retire
     int n_express = 0;
@@ -278,7 +292,7 @@ void run_slot(hg_server& s, Slot& sl) {
       cuda_check(cudaMemcpyAsync(sj.out, cur, (size_t)k.S * 4, cudaMemcpyDeviceToDevice, st), "copy");
     }
     while (n > 1) {
-      const int chunk = (int)std::min<size_t>(64, std::max<size_t>(2, (n + 4095) / 4096));
+      const int chunk = hg::reduce_tree_chunk(k.S, n, s.sms);
       const size_t on = hg::reduce_tree_outputs(k.S, n, chunk);
       uint32_t* dst = on == 1 ? sj.out : sj.bufs[which];
       cuda_check(hg::launch_reduce_tree(k.S, k.kc, cur, n, chunk, dst, err, st), "reduce");
@@ -286,6 +300,10 @@ void run_slot(hg_server& s, Slot& sl) {
       n = on;
       which ^= 1;
     }
+  }
+  if (sl.traced) {
+    if (specs.empty()) cuda_check(cudaEventRecord(sl.tev[1], st), "trace event");
+    cuda_check(cudaEventRecord(sl.tev[2], st), "trace event");
   }
   for (auto& p : posts) {
     cuda_check(cudaMemcpyAsync(static_cast<uint8_t*>(p.q->r.out) + p.out_off, p.dev_out, p.bytes,
@@ -298,7 +316,39 @@ void run_slot(hg_server& s, Slot& sl) {
   }
   sl.err_host = sl.pin.take<uint32_t>(4);
   cuda_check(cudaMemcpyAsync(sl.err_host, err, 4, cudaMemcpyDeviceToHost, st), "D2H err");
+  if (sl.traced) cuda_check(cudaEventRecord(sl.tev[3], st), "trace event");
   cuda_check(cudaEventRecord(sl.ev, st), "event");
+}
+
+double since(std::chrono::steady_clock::time_point t0) {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
+// One trace record of a retired batch (under the lock): slot, class,
+// slices, elements, op mask (bit per op), the host times at which the batch
+// was formed, launched and retired (seconds since the trace started), the
+// GPU time at which its stream started it (seconds since the trace's
+// reference event), and the milliseconds its stream spent on staged copies,
+// on the kernels and on the copies back.
+void trace_retire(hg_server& s, Slot& sl) {
+  std::array<double, kTraceFields> r{};
+  int idx = 0;
+  for (size_t i = 0; i < s.slots.size(); ++i)
+    if (s.slots[i].get() == &sl) idx = (int)i;
+  r[0] = idx;
+  for (int i = 0; i < 4; ++i) r[1 + i] = sl.tr[i];
+  r[5] = sl.tr[4];
+  r[6] = sl.tr[5];
+  r[7] = since(s.trace_t0);
+  float ms = -1.0f;
+  if (cudaEventElapsedTime(&ms, s.trace_ref, sl.tev[0]) != cudaSuccess) ms = -1.0f;
+  r[8] = ms * 1e-3;
+  for (int i = 0; i < 3; ++i) {
+    if (cudaEventElapsedTime(&ms, sl.tev[i], sl.tev[i + 1]) != cudaSuccess) ms = -1.0f;
+    r[9 + i] = ms;
+  }
+  if (s.traces.size() < ((size_t)1 << 20)) s.traces.push_back(r);
+  sl.traced = false;
 }
 
 void finish_req(hg_server& s, Req* q) {
@@ -309,18 +359,17 @@ void finish_req(hg_server& s, Req* q) {
 }
 
 // Class of a pending request: 0 regular, 1 express, 2 slow express.
-// With express_len, short = at most express_len elements; short requests
-// whose batch would wait for a long dependent chain or a host step (CRT
-// decryptions, Mul with a negative scalar, which ends with a host
-// inversion) get the second express slot when there is one, so a batch of
-// the other short ops never waits for them.  Without express_len, short =
-// estimated remaining work <= express_us.
+// With express_len, short = at most express_len elements; short CRT
+// decryptions (a chain of ~2,400 dependent Montgomery steps, several ms even
+// on an idle GPU) get the second express slot when there is one, so a batch
+// of the other short ops never waits for them.  Without express_len, short
+// = estimated remaining work <= express_us.
 int req_class(const hg_server& s, const Req* q) {
   if (s.express_len > 0) {
     if (q->r.count > s.express_len) return 0;
     bool dec_slot = false;
     for (auto& slp : s.slots) dec_slot |= slp->express_dec;
-    return (dec_slot && (q->r.op == hg::kBatchDecrypt || q->neg_scalar)) ? 2 : 1;
+    return (dec_slot && q->r.op == hg::kBatchDecrypt) ? 2 : 1;
   }
   if (s.express_us < 0.0) return 0;
   const double rem = elem_cost_us(*q->k, q->r.op) * (double)(q->r.count - q->next);
@@ -357,6 +406,7 @@ void scheduler(hg_server* sp, int which) {
         if (--q->outstanding == 0 && q->next == q->r.count) finish_req(s, q);
       }
       s.inflight -= sl.bytes;
+      if (sl.traced) trace_retire(s, sl);
       sl.slices.clear();
       sl.busy = false;
     }
@@ -458,10 +508,21 @@ void scheduler(hg_server* sp, int which) {
       sl.bytes = bytes;
       sl.busy = true;
       ++s.batches;
+      sl.traced = s.trace && sl.tev[0];
+      if (sl.traced) {
+        int mask = 0;
+        for (const Slice& sc : sl.slices) mask |= 1 << sc.q->r.op;
+        sl.tr[0] = slot_class;
+        sl.tr[1] = (double)sl.slices.size();
+        sl.tr[2] = (double)elems;
+        sl.tr[3] = mask;
+        sl.tr[4] = since(s.trace_t0);
+      }
       lk.unlock();
       try {
         run_slot(s, sl);
         const auto now = std::chrono::steady_clock::now();
+        if (sl.traced) sl.tr[5] = since(s.trace_t0);
         for (Slice& sc : sl.slices)
           if (sc.start == 0) sc.q->t_launch = now;
       } catch (const HgError& e) {
@@ -475,6 +536,7 @@ void scheduler(hg_server* sp, int which) {
         s.inflight -= bytes;
         sl.slices.clear();
         sl.busy = false;
+        sl.traced = false;
         lk.unlock();
       }
       if (!lk.owns_lock()) lk.lock();

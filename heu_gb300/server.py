@@ -67,6 +67,25 @@ class Server:
                                             ctypes.byref(p)))
         return {"completed": c.value, "batches": b.value, "inflight_bytes": i.value, "pending": p.value}
 
+    def trace_start(self):
+        """Start a per-batch trace (clears the previous one)."""
+        capi.check(self.lib.hg_probe_server_trace(self.handle, 1, None, 0, None))
+
+    def trace_stop(self):
+        """Stop the trace; returns one row per retired batch (a (batches, 12)
+        float64 array): slot, class (0 regular, 1 express, 2 slow express),
+        slices, elements, op mask (bit per op), host times formed / launched /
+        retired and the GPU start time (seconds since trace_start), and the
+        milliseconds the slot's stream spent on staged copies, kernels and
+        copies back."""
+        n = ctypes.c_size_t()
+        capi.check(self.lib.hg_probe_server_trace(self.handle, 0, None, 0, ctypes.byref(n)))
+        recs = np.zeros((n.value, 12), dtype=np.float64)
+        if n.value:
+            capi.check(self.lib.hg_probe_server_trace(self.handle, 0, ctypes.c_void_p(recs.ctypes.data), n.value,
+                                                      ctypes.byref(n)))
+        return recs
+
     def close(self):
         if self.handle:
             self.lib.hg_server_destroy(self.handle)

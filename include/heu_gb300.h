@@ -263,7 +263,12 @@ int hg_batch_wait(hg_batch* b, void* stream);
  * into the next free slot while earlier ones are still on the GPU, and
  * every pending request gets a slice of each micro-batch (processor
  * sharing).  Each result is bit-identical to the same request run alone.  Configure keys
- * (hg_key_set_config / hg_autotune) before creating the server.           */
+ * (hg_key_set_config / hg_autotune) before creating the server.
+ * Every slot's stream needs a hardware work queue of its own, or a slot
+ * waits behind another slot's kernels: hg_ctx_create sets
+ * CUDA_DEVICE_MAX_CONNECTIONS=32 unless it is set, which takes effect only
+ * when that call creates the process's CUDA context (set it before the
+ * first CUDA call otherwise).                                              */
 typedef struct hg_server hg_server;
 #define HG_OP_SUM 4
 typedef struct {
@@ -294,13 +299,13 @@ typedef struct {
                              elements run in the express slots, in the
                              latency layout of the batch kernel (a warp per
                              ciphertext), each batch as soon as a slot is
-                             free; with slots >= 3 short decryptions and
-                             short Muls with a negative scalar (which end
-                             with a host inversion) get an express slot of
-                             their own (slot 1), so the other short requests
-                             never wait for a CRT chain or a host step;
-                             a scheduler thread of their own stages and
-                             launches the express batches */
+                             free; with slots >= 3 short decryptions get an
+                             express slot of their own (slot 1), so the
+                             other short requests never wait for a CRT
+                             chain; each express slot has a scheduler
+                             thread of its own that stages and launches its
+                             batches (and inverts a Mul's negative scalars
+                             on that thread) */
 } hg_server_config;
 #define HG_POLICY_SHORTEST 0
 #define HG_POLICY_FIFO 1

@@ -61,6 +61,18 @@ typedef struct {
 int hg_probe_serve_load(hg_server* s, const hg_load_spec* spec, double* latencies, int* ops, uint64_t* lens,
                         double* wall_s);
 
+/* Per-batch trace of the request server.  enable != 0 clears the trace and
+ * starts recording (records, cap ignored); enable == 0 stops recording,
+ * sets *n to the number of records and copies up to `cap` of them.  A record
+ * is 12 doubles: slot index, class (0 regular, 1 express, 2 slow express),
+ * slices, elements, op mask (bit per op: 0 encrypt, 1 decrypt, 2 add, 3 mul,
+ * 4 sum), the host times (seconds since the trace started) at which the
+ * batch was formed, launched and retired, the GPU time (seconds since a
+ * reference event recorded when the trace started) at which its stream began
+ * the batch, and the milliseconds its stream spent on staged copies, on the
+ * kernels and on the copies back. */
+int hg_probe_server_trace(hg_server* s, int enable, double* records, size_t cap, size_t* n);
+
 #ifdef __cplusplus
 }
 #endif

@@ -77,6 +77,8 @@ def test_served_results_equal_alone(gpu_ctx, gpu_key, policy, express_len):
             in1 = None if h1 else q["x1"]
             tickets[i] = server.submit(q["key"], q["op"], q["n"], in0=in0, in1=in1, h0=h0, h1=h1, out=q["out"])
 
+    b0 = server.stats()["batches"]
+    server.trace_start()
     ths = [threading.Thread(target=submit, args=(list(range(t, len(reqs), 4)),)) for t in range(4)]
     for t in ths:
         t.start()
@@ -86,6 +88,16 @@ def test_served_results_equal_alone(gpu_ctx, gpu_key, policy, express_len):
     assert all(v >= 0 for v in lats)
     st = server.stats()
     assert st["completed"] == len(reqs) and st["pending"] == 0
+    # one trace record per batch, in the classes this configuration has
+    tr = server.trace_stop()
+    assert len(tr) == st["batches"] - b0
+    assert set(np.unique(tr[:, 1])) <= ({0, 1, 2} if express_len else {0})
+    if express_len:
+        assert (tr[tr[:, 1] > 0, 3] <= express_len).all()
+        assert (tr[tr[:, 1] == 2, 4] == 2).all()  # the slow express slot runs decryptions only
+    assert (tr[:, 3] >= 1).all() and (tr[:, 4] > 0).all()
+    assert (tr[:, 5] <= tr[:, 6]).all() and (tr[:, 6] <= tr[:, 7]).all()
+    assert (tr[:, 9:12] >= 0).all()
     for q in reqs:
         x0 = q["x0"]
         x1 = q["x1"]
