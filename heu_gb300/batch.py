@@ -12,6 +12,7 @@ import ctypes
 from heu_gb300 import capi
 
 ENCRYPT, DECRYPT, ADD, MUL = capi.HG_OP_ENCRYPT, capi.HG_OP_DECRYPT, capi.HG_OP_ADD, capi.HG_OP_MUL
+PER_KEY = capi.HG_BATCH_PER_KEY
 
 
 def _addr(x):
@@ -51,6 +52,8 @@ class Batch:
         self.jobs = []
 
     def set_variant(self, variant):
+        """0 or 1: every job in that layout variant set; PER_KEY: each job in
+        its key's tuned layout, one persistent launch per set in use."""
         capi.check(self.lib.hg_batch_set_variant(self.handle, variant))
 
     def run(self, stream=None, graph=False):

@@ -127,6 +127,7 @@ _lib = None
 HG_OP_ENCRYPT, HG_OP_DECRYPT, HG_OP_ADD, HG_OP_MUL, HG_OP_SUM = 0, 1, 2, 3, 4
 HG_CODEC_PLAIN_I64, HG_CODEC_PLAIN_F64, HG_CODEC_BATCH_I64, HG_CODEC_BATCH_F64 = 1, 2, 3, 4
 HG_JOB_NONNEG = 1
+HG_BATCH_PER_KEY = -1
 
 
 class ServerConfig(ctypes.Structure):

@@ -2265,12 +2265,18 @@ struct hg_batch {
   hg_ctx* ctx = nullptr;
   std::vector<Job> jobs;
   bool dirty = true;
-  int variant = 0;
-  DevBuf djobs, dtiles, dcounter, derr, dscratch;
+  int variant = 0;  // variant set of every job, or HG_BATCH_PER_KEY
+  // one persistent launch per variant set in use (one unless per key)
+  struct Group {
+    int V = 0;
+    DevBuf djobs, dtiles, dcounter;
+    uint32_t ntiles = 0;
+    size_t warp_words = 0;
+    int grid = 0;
+  };
+  std::vector<std::unique_ptr<Group>> groups;
+  DevBuf derr, dscratch;
   PinBuf pin_err;
-  uint32_t ntiles = 0;
-  size_t warp_words = 0;
-  int grid = 0;
   struct Inv {
     KeyRec* key;
     size_t job;
@@ -2395,20 +2401,37 @@ void batch_build(hg_batch& b) {
       b.invs.push_back(std::move(inv));
     }
   }
-  const BatchPlan plan = plan_batch(specs, V);
-  auto* jd = b.djobs.ensure<hg::BatchJob>(std::max<size_t>(plan.jobs.size(), 1) * sizeof(hg::BatchJob));
-  auto* td = b.dtiles.ensure<hg::BatchTile>(std::max<size_t>(plan.tiles.size(), 1) * sizeof(hg::BatchTile));
-  if (!plan.jobs.empty())
-    cuda_check(cudaMemcpy(jd, plan.jobs.data(), plan.jobs.size() * sizeof(hg::BatchJob), cudaMemcpyHostToDevice),
-               "jobs");
-  if (!plan.tiles.empty())
-    cuda_check(cudaMemcpy(td, plan.tiles.data(), plan.tiles.size() * sizeof(hg::BatchTile), cudaMemcpyHostToDevice),
-               "tiles");
-  b.ntiles = (uint32_t)plan.tiles.size();
-  b.warp_words = plan.warp_words;
-  b.grid = hg::batch_resident_blocks(V);
-  b.dscratch.ensure<uint32_t>((size_t)b.grid * hg::batch_warps_per_block() * plan.warp_words * 4);
-  b.dcounter.ensure<uint32_t>(4);
+  // the jobs of each variant set: all of them, or per key its tuned layout
+  // (the decryption layout for decryptions, the mod n^2 layout otherwise)
+  std::map<int, std::vector<JobSpec>> by_v;
+  for (const JobSpec& J : specs) {
+    const int jv = V >= 0 ? V : (J.op == hg::kBatchDecrypt ? J.k->sc.variant : J.k->kc.variant);
+    by_v[jv].push_back(J);
+  }
+  b.groups.clear();
+  size_t scratch_words = 1;
+  for (auto& kv : by_v) {
+    auto g = std::make_unique<hg_batch::Group>();
+    g->V = kv.first;
+    const BatchPlan plan = plan_batch(kv.second, g->V);
+    auto* jd = g->djobs.ensure<hg::BatchJob>(std::max<size_t>(plan.jobs.size(), 1) * sizeof(hg::BatchJob));
+    auto* td = g->dtiles.ensure<hg::BatchTile>(std::max<size_t>(plan.tiles.size(), 1) * sizeof(hg::BatchTile));
+    if (!plan.jobs.empty())
+      cuda_check(cudaMemcpy(jd, plan.jobs.data(), plan.jobs.size() * sizeof(hg::BatchJob), cudaMemcpyHostToDevice),
+                 "jobs");
+    if (!plan.tiles.empty())
+      cuda_check(
+          cudaMemcpy(td, plan.tiles.data(), plan.tiles.size() * sizeof(hg::BatchTile), cudaMemcpyHostToDevice),
+          "tiles");
+    g->ntiles = (uint32_t)plan.tiles.size();
+    g->warp_words = plan.warp_words;
+    g->grid = hg::batch_resident_blocks(g->V);
+    g->dcounter.ensure<uint32_t>(4);
+    scratch_words = std::max(scratch_words, (size_t)g->grid * hg::batch_warps_per_block() * plan.warp_words);
+    b.groups.push_back(std::move(g));
+  }
+  // the launches run one after another on the stream, so they share scratch
+  b.dscratch.ensure<uint32_t>(scratch_words * 4);
   b.derr.ensure<uint32_t>(4);
   b.pin_err.ensure<uint32_t>(4);
   // size the inversion trees now so nothing allocates during a capture
@@ -2421,11 +2444,14 @@ void batch_build(hg_batch& b) {
 
 void batch_enqueue(hg_batch& b, cudaStream_t st) {
   uint32_t* err = b.derr.as<uint32_t>();
-  cuda_check(cudaMemsetAsync(b.dcounter.p, 0, 4, st), "memset counter");
   cuda_check(cudaMemsetAsync(err, 0, 4, st), "memset err");
-  cuda_check(hg::launch_batch(b.variant, b.djobs.as<hg::BatchJob>(), b.dtiles.as<hg::BatchTile>(), b.ntiles,
-                              b.dcounter.as<uint32_t>(), b.dscratch.as<uint32_t>(), b.warp_words, err, b.grid, st),
-             "batch launch");
+  for (auto& g : b.groups) {
+    cuda_check(cudaMemsetAsync(g->dcounter.p, 0, 4, st), "memset counter");
+    cuda_check(hg::launch_batch(g->V, g->djobs.as<hg::BatchJob>(), g->dtiles.as<hg::BatchTile>(), g->ntiles,
+                                g->dcounter.as<uint32_t>(), b.dscratch.as<uint32_t>(), g->warp_words, err, g->grid,
+                                st),
+               "batch launch");
+  }
   for (auto& inv : b.invs) {
     const auto& J = b.jobs[inv->job];
     inv->task.status = 0;
@@ -2616,7 +2642,8 @@ int hg_batch_clear(hg_batch* b) {
 
 int hg_batch_set_variant(hg_batch* b, int variant) {
   return guarded(__func__, [&] {
-    if (!b || variant < 0 || variant > 1) fail(HG_ERR_INVALID, "variant must be 0 or 1");
+    if (!b || (variant != HG_BATCH_PER_KEY && (variant < 0 || variant > 1)))
+      fail(HG_ERR_INVALID, "variant must be 0, 1 or HG_BATCH_PER_KEY");
     if (variant != b->variant) {
       b->variant = variant;
       b->dirty = true;
@@ -2748,9 +2775,12 @@ int hg_server_create(hg_ctx* ctx, const hg_server_config* cfg, hg_server** out) 
     for (int i = 0; i < c.slots; ++i) {
       auto sl = std::make_unique<Slot>();
       sl->express = (i == 0 && s->express_us >= 0.0);
-      // a second express slot for short decryptions (latency class by length)
+      // the length rule: an express slot for short decryptions (slot 1), and
+      // with five slots or more a second one for the other short requests
+      // (slot 2), so a short request does not wait for the batch before it
       sl->express_dec = (i == 1 && s->express_len > 0 && c.slots >= 3);
       if (sl->express_dec) sl->express = true;
+      if (i == 2 && s->express_len > 0 && c.slots >= 5) sl->express = true;
       int lo_prio = 0, hi_prio = 0;
       cuda_check(cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio), "priority range");
       cuda_check(cudaStreamCreateWithPriority(&sl->st, cudaStreamNonBlocking, sl->express ? hi_prio : lo_prio),
@@ -2768,11 +2798,9 @@ int hg_server_create(hg_ctx* ctx, const hg_server_config* cfg, hg_server** out) 
     }
     hg_server* raw = s.get();
     if (s->express_len > 0) {
-      s->sched = std::thread(scheduler, raw, 0);
-      s->sched_express = std::thread(scheduler, raw, 1);
-      bool dec_slot = false;
-      for (auto& sl : s->slots) dec_slot |= sl->express_dec;
-      if (dec_slot) s->sched_express_slow = std::thread(scheduler, raw, 2);
+      s->sched = std::thread(scheduler, raw, kRegularSlots);
+      for (size_t i = 0; i < s->slots.size(); ++i)
+        if (s->slots[i]->express) s->sched_express.emplace_back(scheduler, raw, (int)i);
     } else {
       s->sched = std::thread(scheduler, raw, -1);
     }
@@ -2790,8 +2818,8 @@ int hg_server_destroy(hg_server* s) {
     }
     s->cv_work.notify_all();
     if (s->sched.joinable()) s->sched.join();
-    if (s->sched_express.joinable()) s->sched_express.join();
-    if (s->sched_express_slow.joinable()) s->sched_express_slow.join();
+    for (auto& t : s->sched_express)
+      if (t.joinable()) t.join();
     cudaSetDevice(s->ctx->device);
     for (auto& sl : s->slots) {
       cudaStreamSynchronize(sl->st);

@@ -82,6 +82,7 @@ struct Slot {
   cudaEvent_t tev[4] = {nullptr, nullptr, nullptr, nullptr};
   bool traced = false;
   double tr[6] = {0, 0, 0, 0, 0, 0};  // class, slices, elems, op mask, formed, launched
+  std::chrono::steady_clock::time_point t_launched;  // host time the batch was queued
 };
 
 // Fields of one trace record (hg_probe_server_trace).
@@ -133,9 +134,8 @@ struct hg_server {
   int sms = 1;                 // multiprocessors of the server's device
   size_t regular_smem = 0;     // dynamic shared memory that keeps regular batches
                                // off the express slot's blocks on every SM
-  std::thread sched;
-  std::thread sched_express;       // the express slot's scheduler (length rule)
-  std::thread sched_express_slow;  // the slow express slot's scheduler
+  std::thread sched;                      // every slot, or the regular slots (length rule)
+  std::vector<std::thread> sched_express;  // one per express slot (length rule)
   bool trace = false;              // record one trace record per retired batch
   std::chrono::steady_clock::time_point trace_t0;
   cudaEvent_t trace_ref = nullptr;  // GPU time zero of the trace
@@ -277,6 +277,9 @@ void run_slot(hg_server& s, Slot& sl) {
                                 sl.express ? 0 : s.regular_smem),
                "batch launch");
   }
+  // launched: the staged copies and the batch kernel are queued (the
+  // inversions below may wait for the kernel on this thread)
+  sl.t_launched = std::chrono::steady_clock::now();
   for (auto& iv : invs) {
     iv.task->status = 0;
     // express batches invert on their own scheduler thread (see
@@ -376,15 +379,26 @@ int req_class(const hg_server& s, const Req* q) {
   return rem <= s.express_us ? 1 : 0;
 }
 
-// One scheduler thread serves the regular slots (which = 0) and, with the
-// length rule, one thread each express slot (which = 1: the express slot,
-// 2: the slow express slot), so short requests are staged and launched
+// Scheduler threads: which = -1 serves every slot (one thread, no length
+// rule); with the length rule one thread serves the regular slots
+// (which = kRegularSlots) and every express slot has a thread of its own
+// (which = the slot's index), so a short batch is staged and launched
 // without waiting for the host work (staging, planning, inversions) of
-// another batch; which = -1 serves every slot.
-bool serves(const Slot& sl, int which) {
-  if (which < 0) return true;
-  if (which == 0) return !sl.express;
-  return sl.express && (sl.express_dec == (which == 2));
+// another batch.
+constexpr int kRegularSlots = -2;
+
+bool serves(const hg_server& s, const Slot& sl, int which) {
+  if (which == -1) return true;
+  if (which == kRegularSlots) return !sl.express;
+  return (size_t)which < s.slots.size() && s.slots[(size_t)which].get() == &sl;
+}
+
+// Request class a scheduler thread admits (-1: any).
+int thread_class(const hg_server& s, int which) {
+  if (which == -1) return -1;
+  if (which == kRegularSlots) return 0;
+  const Slot& sl = *s.slots[(size_t)which];
+  return sl.express_dec ? 2 : 1;
 }
 
 void scheduler(hg_server* sp, int which) {
@@ -395,7 +409,7 @@ void scheduler(hg_server* sp, int which) {
     // retire finished slots
     for (auto& slp : s.slots) {
       Slot& sl = *slp;
-      if (!sl.busy || !serves(sl, which)) continue;
+      if (!sl.busy || !serves(s, sl, which)) continue;
       if (cudaEventQuery(sl.ev) != cudaSuccess) continue;
       const uint32_t bits = *sl.err_host;
       for (Slice& sc : sl.slices) {
@@ -412,7 +426,7 @@ void scheduler(hg_server* sp, int which) {
     }
     if (s.stop && s.pending.empty()) {
       bool any = false;
-      for (auto& slp : s.slots) any |= slp->busy && serves(*slp, which);
+      for (auto& slp : s.slots) any |= slp->busy && serves(s, *slp, which);
       if (!any) break;
     }
     // admit: every pending request gets a slice of at most slice_us of work
@@ -442,7 +456,7 @@ void scheduler(hg_server* sp, int which) {
     const size_t express_batch_elems = s.express_len > 0 ? s.express_len : s.cfg.max_batch_elems;
     for (auto& slp : s.slots) {
       Slot& sl = *slp;
-      if (sl.busy || s.pending.empty() || !serves(sl, which)) continue;
+      if (sl.busy || s.pending.empty() || !serves(s, sl, which)) continue;
       size_t elems = 0, bytes = 0;
       double cost = 0.0;
       const double batch_cap = sl.express ? express_batch_us : s.batch_us;
@@ -521,10 +535,9 @@ void scheduler(hg_server* sp, int which) {
       lk.unlock();
       try {
         run_slot(s, sl);
-        const auto now = std::chrono::steady_clock::now();
-        if (sl.traced) sl.tr[5] = since(s.trace_t0);
+        if (sl.traced) sl.tr[5] = std::chrono::duration<double>(sl.t_launched - s.trace_t0).count();
         for (Slice& sc : sl.slices)
-          if (sc.start == 0) sc.q->t_launch = now;
+          if (sc.start == 0) sc.q->t_launch = sl.t_launched;
       } catch (const HgError& e) {
         cudaStreamSynchronize(sl.st);
         lk.lock();
@@ -544,14 +557,15 @@ void scheduler(hg_server* sp, int which) {
     }
     if (!launched) {
       bool any_busy = false;
-      for (auto& slp : s.slots) any_busy |= slp->busy && serves(*slp, which);
+      for (auto& slp : s.slots) any_busy |= slp->busy && serves(s, *slp, which);
       // poll busy slots quickly; sleep when idle until work of this thread's
       // slots arrives (with the length rule each thread waits for its class)
+      const int cls = thread_class(s, which);
       auto mine = [&] {
         if (s.stop) return true;
-        if (which < 0 || s.express_len == 0) return !s.pending.empty();
+        if (cls < 0 || s.express_len == 0) return !s.pending.empty();
         for (const Req* q : s.pending)
-          if (req_class(s, q) == which) return true;
+          if (req_class(s, q) == cls) return true;
         return false;
       };
       if (any_busy)

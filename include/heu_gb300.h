@@ -249,6 +249,11 @@ int hg_batch_destroy(hg_batch* b);
 int hg_batch_add(hg_batch* b, int key_id, int op, size_t count, const void* in0, const void* in1, void* out,
                  void* aux, int flags);
 int hg_batch_clear(hg_batch* b);
+/* Layout variant set of the batch's kernel: 0 or 1 for every job (default
+ * 0), or HG_BATCH_PER_KEY: every job in its key's tuned layout
+ * (hg_key_config: dec_variant for decryptions, variant for the other ops),
+ * run as one persistent launch per variant set in use, back to back.    */
+#define HG_BATCH_PER_KEY (-1)
 int hg_batch_set_variant(hg_batch* b, int variant);
 int hg_batch_run(hg_batch* b, void* stream, int use_graph);
 int hg_batch_wait(hg_batch* b, void* stream);
@@ -302,10 +307,12 @@ typedef struct {
                              free; with slots >= 3 short decryptions get an
                              express slot of their own (slot 1), so the
                              other short requests never wait for a CRT
-                             chain; each express slot has a scheduler
-                             thread of its own that stages and launches its
-                             batches (and inverts a Mul's negative scalars
-                             on that thread) */
+                             chain, and with slots >= 5 the other short
+                             requests get two (slots 0 and 2), so one does
+                             not wait for the batch before it; each express
+                             slot has a scheduler thread of its own that
+                             stages and launches its batches (and inverts a
+                             Mul's negative scalars on that thread) */
 } hg_server_config;
 #define HG_POLICY_SHORTEST 0
 #define HG_POLICY_FIFO 1

@@ -98,6 +98,33 @@ def test_batch_matches_per_call_eager_and_graph(gpu_ctx, gpu_key, variant):
     batch.close()
 
 
+def test_batch_per_key_variants(gpu_ctx, gpu_key):
+    """HG_BATCH_PER_KEY: each job in its key's tuned layout (decryptions in
+    the key's dec_variant), one launch per variant set; results unchanged."""
+    torch = pytest.importorskip("torch")
+    keys = [gpu_key(b, s)[0] for b, s in KEYS]
+    saved = [autotune.get_config(k) for k in keys]
+    try:
+        # both variant sets in use, crossed between the n^2 and p^2 layouts
+        for k, (v, dv) in zip(keys, [(1, 0), (0, 1), (1, 1)]):
+            autotune.set_config(k, dict(autotune.get_config(k), variant=v, dec_variant=dv))
+        jobs = _build_jobs(torch, keys, [300, 129, 70])
+        batch = hg.Batch(gpu_ctx)
+        batch.set_variant(hg.batch.PER_KEY)
+        _fill(batch, jobs)
+        batch.run(graph=False)
+        batch.wait()
+        _check(torch, jobs)
+        _zero(jobs)
+        batch.run(graph=True)
+        batch.wait()
+        _check(torch, jobs)
+        batch.close()
+    finally:
+        for k, c in zip(keys, saved):
+            autotune.set_config(k, c)
+
+
 def test_batch_reports_range_errors(gpu_ctx, gpu_key):
     torch = pytest.importorskip("torch")
     key, pk, sk = gpu_key(1024, 1)

@@ -31,11 +31,12 @@ def _alone(key, op, x0, x1):
                                                  (hg.Server.SHORTEST, 512)],
                          ids=["shortest", "fifo", "latency-class"])
 def test_served_results_equal_alone(gpu_ctx, gpu_key, policy, express_len):
-    """With express_len the requests of at most 512 elements run in the two
-    express slots in the latency layout; results stay identical."""
+    """With express_len the requests of at most 512 elements run in the three
+    express slots (one for short decryptions, two for the other short
+    requests) in the latency layout; results stay identical."""
     keys = [gpu_key(2048, 0)[0], gpu_key(3072, 2)[0], gpu_key(1024, 1)[0]]
     rng = np.random.default_rng(17)
-    server = hg.Server(gpu_ctx, budget_bytes=2 << 30, slots=4 if express_len else 3, max_batch_elems=1 << 14,
+    server = hg.Server(gpu_ctx, budget_bytes=2 << 30, slots=5 if express_len else 3, max_batch_elems=1 << 14,
                        policy=policy, express_len=express_len)
     # one resident vector per key
     vec_len = 3000
@@ -95,6 +96,8 @@ def test_served_results_equal_alone(gpu_ctx, gpu_key, policy, express_len):
     if express_len:
         assert (tr[tr[:, 1] > 0, 3] <= express_len).all()
         assert (tr[tr[:, 1] == 2, 4] == 2).all()  # the slow express slot runs decryptions only
+        assert set(np.unique(tr[tr[:, 1] == 1, 0])) <= {0, 2}  # the two express slots of the rest
+        assert set(np.unique(tr[tr[:, 1] == 0, 0])) <= {3, 4}
     assert (tr[:, 3] >= 1).all() and (tr[:, 4] > 0).all()
     assert (tr[:, 5] <= tr[:, 6]).all() and (tr[:, 6] <= tr[:, 7]).all()
     assert (tr[:, 9:12] >= 0).all()
