@@ -8,8 +8,10 @@ fastest.  The configuration never changes results, only speed.
 """
 
 import ctypes
+import fcntl
 import json
 import os
+import tempfile
 
 from heu_gb300 import capi
 
@@ -46,21 +48,31 @@ def set_config(key, config):
 
 
 def save(config, key_bits, path=DEFAULT_CACHE, device=0, rates=None):
-    data = {}
-    if os.path.exists(path):
-        try:
-            data = json.load(open(path))
-        except (OSError, ValueError):
-            data = {}
-    entry = {"config": config}
-    if rates:
-        entry["rates"] = rates
-    data.setdefault(device_name(device), {})[str(key_bits)] = entry
+    """Record a key size's configuration in the JSON cache.  The
+    read-modify-replace runs under an exclusive lock on a side file, so
+    processes and threads saving at once keep each other's entries; the new
+    file is written under a unique temporary name and renamed into place."""
     os.makedirs(os.path.dirname(path) or ".", exist_ok=True)
-    tmp = f"{path}.{os.getpid()}.tmp"  # processes saving at once each replace the file whole
-    with open(tmp, "w") as f:
-        json.dump(data, f, indent=1, sort_keys=True)
-    os.replace(tmp, path)
+    with open(path + ".lock", "a") as lock:
+        fcntl.flock(lock, fcntl.LOCK_EX)
+        try:
+            data = {}
+            if os.path.exists(path):
+                try:
+                    data = json.load(open(path))
+                except (OSError, ValueError):
+                    data = {}
+            entry = {"config": config}
+            if rates:
+                entry["rates"] = rates
+            data.setdefault(device_name(device), {})[str(key_bits)] = entry
+            fd, tmp = tempfile.mkstemp(prefix=os.path.basename(path) + ".", suffix=".tmp",
+                                       dir=os.path.dirname(path) or ".")
+            with os.fdopen(fd, "w") as f:
+                json.dump(data, f, indent=1, sort_keys=True)
+            os.replace(tmp, path)
+        finally:
+            fcntl.flock(lock, fcntl.LOCK_UN)
 
 
 def load(key_bits, path=DEFAULT_CACHE, device=0):

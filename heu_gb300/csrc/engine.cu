@@ -2362,7 +2362,10 @@ BatchPlan plan_batch(const std::vector<JobSpec>& specs, int V) {
       if (J.op == hg::kBatchMul)
         plan.warp_words = std::max(plan.warp_words, (size_t)per_pass * ((size_t)1 << (k->wm - 1)) * k->S);
     }
-    const size_t tile = (size_t)per_pass * 4;
+    // a throughput tile is four passes of a warp (fewer trips to the
+    // queue); a latency tile one pass, so a short batch spreads one chain
+    // per warp instead of queueing four chains behind each other on a warp
+    const size_t tile = (size_t)per_pass * (V == hg::kBatchLatencyVariant ? 1 : 4);
     const double c = job_cost(*k, J.op);
     for (size_t st = 0; st < J.count; st += tile) {
       const size_t cnt = std::min(tile, J.count - st);
