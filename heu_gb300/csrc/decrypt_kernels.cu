@@ -10,12 +10,20 @@ namespace hg {
 
 namespace {
 constexpr int kBlock = 128;
-}
+
+// Resident blocks per SM the compiler must fit (register budget).  The
+// 2048-bit throughput layout (4 lanes x 16 limbs per side) is held at 96
+// registers so five blocks fit instead of four: decryption 312 k/s -> 322
+// k/s on 2^20 ciphertexts (the extra warps hide more of the dependent
+// multiply-add latency; six blocks, 80 registers, spill and fall back to
+// 315 k/s).  The other layouts keep the compiler's own budget.
+constexpr int dec_min_blocks(int TP, int LP) { return (TP == 4 && LP == 16) ? 5 : 1; }
+}  // namespace
 
 void count_launches(uint64_t n);
 
 template <int TP, int LP>
-__global__ void __launch_bounds__(kBlock) k_decrypt(KeyConst kc, SecConst sc, const uint32_t* __restrict__ ct,
+__global__ void __launch_bounds__(kBlock, dec_min_blocks(TP, LP)) k_decrypt(KeyConst kc, SecConst sc, const uint32_t* __restrict__ ct,
                                                     size_t count, int64_t* __restrict__ out_i64,
                                                     uint8_t* __restrict__ out_ovf, uint32_t* __restrict__ out_mag,
                                                     uint8_t* __restrict__ out_neg, uint32_t* __restrict__ scratch,
