@@ -3,17 +3,20 @@
 // Included into engine.cu's translation unit: it uses the engine's key
 // records, inversion tasks and batch planner.
 //
-// A scheduler thread owns `slots` in-flight micro-batches, each with its own
-// stream, a device arena, a pinned arena and a scratch buffer for the
-// persistent batch kernel, all sized when the server starts so nothing is
-// allocated while serving.  Requests wait in a FIFO; whenever a slot is free
-// the scheduler admits requests from the front while their device bytes fit
-// the slot's arena and the server-wide budget, stages their host inputs,
-// runs all their encrypt / decrypt / add / mul work in one persistent launch
-// (sums as reduction levels, negative scalars as product trees with a host
-// inversion node), copies the results back and records an event.  Requests
-// that arrive meanwhile are admitted into the next free slot while earlier
-// slots are still on the GPU, so their work overlaps on the device.
+// The server owns `slots` in-flight micro-batches, each with its own stream,
+// a device arena, a pinned arena and a scratch buffer for the persistent
+// batch kernel, all sized when the server starts so nothing is allocated
+// while serving.  Requests wait in a queue; whenever a slot is free its
+// scheduler thread admits requests while their device bytes fit the slot's
+// arena and the server-wide budget, stages their host inputs, runs all their
+// encrypt / decrypt / add / mul work in one persistent launch (sums as tree
+// reduction levels, negative scalars as product trees with a host inversion),
+// copies the results back and records an event.  Requests that arrive
+// meanwhile are admitted into the next free slot while earlier slots are
+// still on the GPU, so their work overlaps on the device.  With the length
+// rule (express_len) short requests go to express slots: each has its own
+// scheduler thread, runs the latency layout of the batch kernel and keeps a
+// share of every SM that the padded regular batches cannot take.
 
 namespace {
 
@@ -129,11 +132,11 @@ struct hg_server {
   int policy = 0;              // HG_POLICY_SHORTEST or HG_POLICY_FIFO
   double express_us = -1.0;    // short-request threshold of the express slot (< 0: none)
   size_t express_len = 0;      // > 0: short = at most this many elements, run in the latency layout
-  int express_grid = 0;        // batch-kernel blocks of the express slot
+  int express_grid = 0;        // batch-kernel blocks of all express slots together
   int regular_grid = 0;        // batch-kernel blocks of every other slot
   int sms = 1;                 // multiprocessors of the server's device
   size_t regular_smem = 0;     // dynamic shared memory that keeps regular batches
-                               // off the express slot's blocks on every SM
+                               // off the express slots' blocks on every SM
   std::thread sched;                      // every slot, or the regular slots (length rule)
   std::vector<std::thread> sched_express;  // one per express slot (length rule)
   bool trace = false;              // record one trace record per retired batch
@@ -262,8 +265,8 @@ void run_slot(hg_server& s, Slot& sl) {
     cuda_check(cudaMemcpyAsync(dt, ht, tb, cudaMemcpyHostToDevice, st), "H2D tiles");
     cuda_check(cudaMemsetAsync(sl.counter.p, 0, 4, st), "memset counter");
     if (sl.traced) cuda_check(cudaEventRecord(sl.tev[1], st), "trace event");
-    // the express slots split the reserved blocks, so neither waits for the
-    // other's blocks to retire
+    // the express slots split the reserved blocks, so none waits for
+    // another's blocks to retire
     int n_express = 0;
     for (auto& o : s.slots) n_express += o->express ? 1 : 0;
     const int grid = sl.express ? std::max(1, s.express_grid / std::max(1, n_express)) : s.regular_grid;
@@ -271,7 +274,7 @@ void run_slot(hg_server& s, Slot& sl) {
       fail(HG_ERR_NOMEM, "server scratch too small for this batch");
     // regular batches carry shared-memory padding that caps them below the
     // per-SM block limit, so however many overlap, every SM keeps room for
-    // the express slot's blocks
+    // the express slots' blocks
     cuda_check(hg::launch_batch(V, dj, dt, (uint32_t)plan.tiles.size(), sl.counter.as<uint32_t>(),
                                 sl.scratch.as<uint32_t>(), plan.warp_words, err, grid, st,
                                 sl.express ? 0 : s.regular_smem),
